@@ -1,0 +1,707 @@
+// RCCSD / DF-RCCSD amplitude iteration on one GPU.
+//
+// Algorithm: Fermi.jl's closed-shell CCSD (src/Methods/CoupledCluster/RCCSD/
+// RCCSDHelper.jl:8-349, driver RCCSDa.jl:92-244, DIIS src/Core/DIIS.jl).  The
+// residual is evaluated in the T1-dressed density-fitted form (Koch et al.,
+// J. Chem. Phys. 100, 4393 (1994); DePrince & Sherrill, J. Chem. Theory
+// Comput. 9, 2687 (2013)): the three-index factors are dressed with T1 once
+// per iteration and every T1 term of the reference equations is carried by
+// them, leaving CCD-like doubles equations.  It is the same function of
+// (T1, T2) as the reference's term-by-term sum (RCCSDHelper.jl:57-192); the
+// test suite checks the two against each other for arbitrary amplitudes.
+//
+// Jacobi update, rms, DIIS cadence and the energy follow RCCSDa.jl exactly;
+// the update, rms, DIIS error vectors and dot products and the energy are one
+// fused bandwidth-bound pass (update_t2_kernel).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "fcc_ctx.cuh"
+
+namespace fcc {
+
+namespace {
+
+constexpr int RED_BLOCKS = 608;  // 152 SMs x 4: fixed, so reductions are deterministic
+constexpr int RED_THREADS = 256;
+constexpr int MAX_DIIS = 8;
+// partial-sum layout per block: [0] sum dT^2, [1] energy, [2..2+MAX_DIIS) dots
+constexpr int NPART = 2 + MAX_DIIS;
+
+__device__ __forceinline__ double warp_sum(double x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  return x;
+}
+
+// Block-reduce NPART values held per thread into part[blockIdx.x*NPART + k].
+__device__ void block_reduce_store(double (&vals)[NPART], int nvals, double* part) {
+  __shared__ double sm[RED_THREADS / 32][NPART];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int k = 0; k < nvals; ++k) {
+    double s = warp_sum(vals[k]);
+    if (lane == 0) sm[w][k] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < nvals) {
+    double s = 0.0;
+    for (int i = 0; i < RED_THREADS / 32; ++i) s += sm[i][threadIdx.x];
+    part[blockIdx.x * NPART + threadIdx.x] = s;
+  }
+}
+
+// Sum the per-block partials (fixed order) into out[k].
+__global__ void finish_reduce_kernel(const double* part, int nblocks, int nvals, double* out) {
+  int k = threadIdx.x;
+  if (k >= nvals) return;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; ++b) s += part[b * NPART + k];
+  out[k] = s;
+}
+
+struct ErrSlots {
+  const float* s[MAX_DIIS];
+  const double* d[MAX_DIIS];
+  int n;
+};
+
+// Fused amplitude update (kernel (c)): for every element
+//   dT = R / D, D = e_i + e_j - e_a - e_b (or e_i - e_a for T1),
+//   Tnew = T + dT, accumulate dT^2, store dT as the DIIS error (FP32 or FP64),
+//   accumulate dot(dT, e_k) with the other stored errors, and the energy
+//   contribution Lt * (Tnew + t1new_ia t1new_jb) (T2 only).
+// rank 2: index e -> (i, a); rank 4: e -> (i, j, a, b), b fastest.
+__global__ void __launch_bounds__(RED_THREADS) update_kernel(
+    int rank, const double* __restrict__ T, const double* __restrict__ R, const double* __restrict__ eps,
+    int o, int v, double* __restrict__ Tnew, float* __restrict__ err_s, double* __restrict__ err_d,
+    ErrSlots others, const double* __restrict__ Lt, const double* __restrict__ t1new, double* part) {
+  const int64_t total = rank == 2 ? (int64_t)o * v : (int64_t)o * o * v * v;
+  double vals[NPART];
+#pragma unroll
+  for (int k = 0; k < NPART; ++k) vals[k] = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // two elements per step with 128-bit loads when the pair is aligned
+  for (int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 2; p < total; p += 2 * stride) {
+    double tv[2], rv[2];
+    int cnt = (p + 1 < total) ? 2 : 1;
+    if (cnt == 2 && ((reinterpret_cast<uintptr_t>(T + p) | reinterpret_cast<uintptr_t>(R + p)) & 15) == 0) {
+      double2 t2v = *reinterpret_cast<const double2*>(T + p);
+      double2 r2v = *reinterpret_cast<const double2*>(R + p);
+      tv[0] = t2v.x; tv[1] = t2v.y; rv[0] = r2v.x; rv[1] = r2v.y;
+    } else {
+      for (int q = 0; q < cnt; ++q) { tv[q] = T[p + q]; rv[q] = R[p + q]; }
+    }
+    double tn[2], dt[2];
+    for (int q = 0; q < cnt; ++q) {
+      int64_t e = p + q;
+      double D;
+      int64_t i, j = 0, a, b = 0;
+      if (rank == 2) {
+        i = e / v; a = e - i * v;
+        D = eps[i] - eps[o + a];
+      } else {
+        b = e % v; int64_t r = e / v;
+        a = r % v; r /= v;
+        j = r % o; i = r / o;
+        D = eps[i] + eps[j] - eps[o + a] - eps[o + b];
+      }
+      dt[q] = rv[q] / D;
+      tn[q] = tv[q] + dt[q];
+      vals[0] += dt[q] * dt[q];
+      if (rank == 4 && Lt) vals[1] += Lt[e] * (tn[q] + t1new[i * v + a] * t1new[j * v + b]);
+      double ev;
+      if (err_s) { float f = (float)dt[q]; err_s[e] = f; ev = (double)f; }
+      else if (err_d) { err_d[e] = dt[q]; ev = dt[q]; }
+      else ev = dt[q];
+      for (int k = 0; k < others.n; ++k) {
+        double oe = others.s[k] ? (double)others.s[k][e] : others.d[k][e];
+        vals[2 + k] += ev * oe;
+      }
+    }
+    if (cnt == 2 && (reinterpret_cast<uintptr_t>(Tnew + p) & 15) == 0) {
+      *reinterpret_cast<double2*>(Tnew + p) = make_double2(tn[0], tn[1]);
+    } else {
+      for (int q = 0; q < cnt; ++q) Tnew[p + q] = tn[q];
+    }
+  }
+  block_reduce_store(vals, 2 + others.n, part);
+}
+
+// Self dot of the stored error (its norm^2 in the stored precision).
+__global__ void __launch_bounds__(RED_THREADS) selfdot_kernel(int64_t total, const float* es, const double* ed,
+                                                              double* part) {
+  double vals[NPART];
+#pragma unroll
+  for (int k = 0; k < NPART; ++k) vals[k] = 0.0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    double x = es ? (double)es[e] : ed[e];
+    vals[0] += x * x;
+  }
+  block_reduce_store(vals, 1, part);
+}
+
+// DIIS extrapolation: out = sum_k c_k (vec_k + add_res * err_k); for T2 also
+// accumulates the energy with the already extrapolated t1.
+struct VecSlots {
+  const double* vec[MAX_DIIS];
+  const float* es[MAX_DIIS];
+  const double* ed[MAX_DIIS];
+  int n;
+};
+
+__global__ void __launch_bounds__(RED_THREADS) extrapolate_kernel(int rank, int o, int v, VecSlots sl,
+                                                                  const double* __restrict__ coef,
+                                                                  double* __restrict__ out,
+                                                                  const double* __restrict__ Lt,
+                                                                  const double* __restrict__ t1new, double* part) {
+  const int64_t total = rank == 2 ? (int64_t)o * v : (int64_t)o * o * v * v;
+  double vals[NPART];
+#pragma unroll
+  for (int k = 0; k < NPART; ++k) vals[k] = 0.0;
+  double c[MAX_DIIS];
+  for (int k = 0; k < sl.n; ++k) c[k] = coef[k];
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < sl.n; ++k) {
+      double ev = sl.es[k] ? (double)sl.es[k][e] : sl.ed[k][e];
+      s += c[k] * sl.vec[k][e] + c[k] * ev;
+    }
+    out[e] = s;
+    if (rank == 4 && Lt) {
+      int64_t b = e % v, r = e / v, a = r % v;
+      r /= v;
+      int64_t j = r % o, i = r / o;
+      vals[1] += Lt[e] * (s + t1new[i * v + a] * t1new[j * v + b]);
+    }
+  }
+  block_reduce_store(vals, 2, part);
+}
+
+// Energy of given amplitudes: sum Lt * (t2 + t1 t1).
+__global__ void __launch_bounds__(RED_THREADS) energy_kernel(int o, int v, const double* __restrict__ t2,
+                                                             const double* __restrict__ t1,
+                                                             const double* __restrict__ Lt, double* part) {
+  const int64_t total = (int64_t)o * o * v * v;
+  double vals[NPART];
+#pragma unroll
+  for (int k = 0; k < NPART; ++k) vals[k] = 0.0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b = e % v, r = e / v, a = r % v;
+    r /= v;
+    int64_t j = r % o, i = r / o;
+    vals[1] += Lt[e] * (t2[e] + t1[i * v + a] * t1[j * v + b]);
+  }
+  block_reduce_store(vals, 2, part);
+}
+
+// Solve the bordered DIIS system B c = (0,..,0,1) in FP64 with partial
+// pivoting (DIIS.jl:66-87); one thread, N <= MAX_DIIS + 1.
+__global__ void diis_solve_kernel(const double* Bm, int N, double* coef, int* status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double A[MAX_DIIS + 1][MAX_DIIS + 2];
+  for (int r = 0; r < N; ++r) {
+    for (int c = 0; c < N; ++c) A[r][c] = Bm[r * N + c];
+    A[r][N] = (r == N - 1) ? 1.0 : 0.0;
+  }
+  int st = 0;
+  for (int col = 0; col < N; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < N; ++r)
+      if (fabs(A[r][col]) > fabs(A[piv][col])) piv = r;
+    if (A[piv][col] == 0.0) { st = 1; break; }
+    if (piv != col)
+      for (int c = 0; c <= N; ++c) { double t = A[col][c]; A[col][c] = A[piv][c]; A[piv][c] = t; }
+    for (int r = col + 1; r < N; ++r) {
+      double f = A[r][col] / A[col][col];
+      for (int c = col; c <= N; ++c) A[r][c] -= f * A[col][c];
+    }
+  }
+  if (!st) {
+    for (int r = N - 1; r >= 0; --r) {
+      double s = A[r][N];
+      for (int c = r + 1; c < N; ++c) s -= A[r][c] * coef[c];
+      coef[r] = s / A[r][r];
+    }
+  }
+  *status = st;
+}
+
+// t2 <- OVOV-derived MP2 numerator / D2 (RCCSDa.jl:53-89); t1 <- 0.
+__global__ void divide_d2_kernel(double* t2, const double* eps, int o, int v) {
+  int64_t total = (int64_t)o * o * v * v;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b = e % v, r = e / v, a = r % v;
+    r /= v;
+    int64_t j = r % o, i = r / o;
+    t2[e] /= (eps[i] + eps[j] - eps[o + a] - eps[o + b]);
+  }
+}
+
+// X = 1 - T, Y = 1 + T^T with T[a,i] = t1[i,a] (n x n, row-major).
+__global__ void dress_mats_kernel(const double* t1, int o, int v, double* X, double* Y) {
+  int n = o + v;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += gridDim.x * blockDim.x) {
+    int p = e / n, q = e % n;
+    double xv = (p == q) ? 1.0 : 0.0, yv = xv;
+    if (p >= o && q < o) xv -= t1[q * v + (p - o)];   // X[a,i] = -t_ia
+    if (p < o && q >= o) yv += t1[p * v + (q - o)];   // Y[i,a] = +t_ia
+    X[e] = xv;
+    Y[e] = yv;
+  }
+}
+
+__global__ void fill_kernel(double* p, int64_t n, double val) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) p[e] = val;
+}
+
+__global__ void add_diag_kernel(double* M, const double* d, int n, double scale) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) M[(int64_t)e * n + e] += scale * d[e];
+}
+
+__global__ void axpby_flat_kernel(double* y, const double* x, int64_t n, double a, double b) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    y[e] = a * y[e] + b * x[e];
+}
+
+int grid_for(int64_t n, int threads = 256) {
+  int64_t b = (n + threads - 1) / threads;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 16));
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------- setup
+// Constant tensors derived once from the three-index factors.
+void setup_integrals(fcc_ctx* c) {
+  cudaStream_t s = c->stream;
+  const int64_t o = c->o, v = c->v, Q = c->Q, n = c->n;
+  TView Bf = rm(c->B.p, {Q, n, n});
+  TView Bov = slice(slice(Bf, 1, 0, o), 2, o, v);
+  c->ovov.alloc(o * v * o * v);
+  c->Lldkc.alloc(o * v * o * v);
+  c->Lt.alloc(o * o * v * v);
+  TView ovov = rm(c->ovov.p, {o, v, o, v});
+  einsum(1.0, "Qkc,Qld->kcld", Bov, Bov, 0.0, ovov, s);
+  TView L = rm(c->Lldkc.p, {o, v, o, v});
+  einsum1(2.0, "ldkc->ldkc", ovov, 0.0, L, s);
+  einsum1(-1.0, "lckd->ldkc", ovov, 1.0, L, s);
+  TView Lt = rm(c->Lt.p, {o, o, v, v});
+  einsum1(2.0, "kcld->klcd", ovov, 0.0, Lt, s);
+  einsum1(-1.0, "kdlc->klcd", ovov, 1.0, Lt, s);
+  c->V2.alloc(o * o * v * v);
+  einsum1(1.0, "kcld->klcd", ovov, 0.0, rm(c->V2.p, {o, o, v, v}), s);
+
+  // one-body part h = diag(eps) - G(B), G_pq = 2 sum_Qk (pq|kk) - (pk|kq)
+  c->h.alloc(n * n);
+  c->F.alloc(n * n);
+  c->Xm.alloc(n * n);
+  c->Ym.alloc(n * n);
+  c->tmpnn.alloc(n * n);
+  c->ones.alloc(std::max<int64_t>(o, 1));
+  c->gam.alloc(Q);
+  fill_kernel<<<1, 256, 0, s>>>(c->ones.p, c->ones.n, 1.0);
+  FCC_CHECK_LAUNCH();
+  TView h = rm(c->h.p, {n, n});
+  // gamma_Q = sum_k B[Q,k,k]
+  TView diag;
+  diag.p = c->B.p; diag.rank = 2; diag.dim[0] = Q; diag.dim[1] = o; diag.str[0] = n * n; diag.str[1] = n + 1;
+  TView onesv = rm(c->ones.p, {o});
+  TView gam = rm(c->gam.p, {Q});
+  einsum(1.0, "Qk,k->Q", diag, onesv, 0.0, gam, s);
+  einsum(-2.0, "Qpq,Q->pq", Bf, gam, 0.0, h, s);
+  einsum(1.0, "Qpk,Qkq->pq", slice(Bf, 2, 0, o), slice(Bf, 1, 0, o), 1.0, h, s);
+  add_diag_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(c->h.p, c->eps.p, (int)n, 1.0);
+  FCC_CHECK_LAUNCH();
+
+  // work tensors
+  c->t1.alloc(o * v);
+  c->t2.alloc(o * o * v * v);
+  c->r1.alloc(o * v);
+  c->r2.alloc(o * o * v * v);
+  c->u.alloc(o * o * v * v);
+  c->P.alloc(o * o * v * v);
+  c->Cint.alloc(o * o * v * v);
+  c->Dint.alloc(o * o * v * v);
+  c->Xo.alloc(o * o * o * o);
+  c->Xq.alloc(Q * o * v);
+  c->Yq.alloc(Q * o * v);
+  c->Fvv.alloc(v * v);
+  c->Foo.alloc(o * o);
+  c->Bt.alloc(Q * n * n);
+  c->red.alloc(RED_BLOCKS * NPART + 64);
+  // ladder: v^3 slab per virtual a, blocks of a sized to ~512 MB
+  int64_t per_a = v * v * v;
+  c->ladder_block = std::max<int64_t>(1, std::min<int64_t>(v, (int64_t)(64ll << 20) / std::max<int64_t>(per_a, 1)));
+  c->Wslab.alloc(c->ladder_block * per_a);
+}
+
+void make_mp2_guess(fcc_ctx* c) {
+  cudaStream_t s = c->stream;
+  const int64_t o = c->o, v = c->v;
+  FCC_CUDA(cudaMemsetAsync(c->t1.p, 0, sizeof(double) * o * v, s));
+  einsum1(1.0, "iajb->ijab", rm(c->ovov.p, {o, v, o, v}), 0.0, rm(c->t2.p, {o, o, v, v}), s);
+  divide_d2_kernel<<<grid_for(o * o * v * v), 256, 0, s>>>(c->t2.p, c->eps.p, (int)o, (int)v);
+  FCC_CHECK_LAUNCH();
+}
+
+double cc_energy(fcc_ctx* c, const double* t1, const double* t2) {
+  cudaStream_t s = c->stream;
+  energy_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>((int)c->o, (int)c->v, t2, t1, c->Lt.p, c->red.p);
+  FCC_CHECK_LAUNCH();
+  double* out = c->red.p + RED_BLOCKS * NPART;
+  finish_reduce_kernel<<<1, 32, 0, s>>>(c->red.p, RED_BLOCKS, 2, out);
+  FCC_CHECK_LAUNCH();
+  double h[2];
+  FCC_CUDA(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, s));
+  FCC_CUDA(cudaStreamSynchronize(s));
+  return h[1];
+}
+
+// ---------------------------------------------------------------- residual
+// Full CCSD residuals r1 = Omega_ia, r2 = Omega_ijab (zero at convergence) for
+// the current t1, t2; the reference's pre-denominator amplitudes are
+// r + D * t (RCCSDHelper.jl:304-349).
+void residual_fp64(fcc_ctx* c) {
+  cudaStream_t s = c->stream;
+  const int64_t o = c->o, v = c->v, Q = c->Q, n = c->n;
+  TView t1 = rm(c->t1.p, {o, v});
+  TView t2 = rm(c->t2.p, {o, o, v, v});
+  TView B = rm(c->B.p, {Q, n, n});
+  TView Bt = rm(c->Bt.p, {Q, n, n});
+  auto blk = [](TView t, int64_t r0, int64_t nr, int64_t c0, int64_t nc) {
+    return slice(slice(t, 1, r0, nr), 2, c0, nc);
+  };
+  TView Boo = blk(B, 0, o, 0, o), Bov = blk(B, 0, o, o, v), Bvo = blk(B, o, v, 0, o), Bvv = blk(B, o, v, o, v);
+  TView Btoo = blk(Bt, 0, o, 0, o), Btov = blk(Bt, 0, o, o, v), Btvo = blk(Bt, o, v, 0, o), Btvv = blk(Bt, o, v, o, v);
+
+  // ---- T1-dressed factors: Bt = X B Y^T blockwise
+  einsum1(1.0, "Qij->Qij", Boo, 0.0, Btoo, s);
+  einsum(1.0, "Qib,jb->Qij", Bov, t1, 1.0, Btoo, s);
+  einsum1(1.0, "Qia->Qia", Bov, 0.0, Btov, s);
+  einsum1(1.0, "Qab->Qab", Bvv, 0.0, Btvv, s);
+  einsum(-1.0, "ka,Qkb->Qab", t1, Bov, 1.0, Btvv, s);
+  einsum1(1.0, "Qai->Qai", Bvo, 0.0, Btvo, s);
+  einsum(-1.0, "ka,Qki->Qai", t1, Boo, 1.0, Btvo, s);
+  einsum(1.0, "Qac,ic->Qai", Btvv, t1, 1.0, Btvo, s);
+
+  // ---- dressed Fock F = X h Y^T + G(Bt)
+  dress_mats_kernel<<<grid_for(n * n), 256, 0, s>>>(c->t1.p, (int)o, (int)v, c->Xm.p, c->Ym.p);
+  FCC_CHECK_LAUNCH();
+  TView X = rm(c->Xm.p, {n, n}), Y = rm(c->Ym.p, {n, n}), H = rm(c->h.p, {n, n});
+  TView tmp = rm(c->tmpnn.p, {n, n}), F = rm(c->F.p, {n, n});
+  einsum(1.0, "pr,rs->ps", X, H, 0.0, tmp, s);
+  einsum(1.0, "ps,qs->pq", tmp, Y, 0.0, F, s);
+  TView diag;
+  diag.p = c->Bt.p; diag.rank = 2; diag.dim[0] = Q; diag.dim[1] = o; diag.str[0] = n * n; diag.str[1] = n + 1;
+  TView gam = rm(c->gam.p, {Q});
+  einsum(1.0, "Qk,k->Q", diag, rm(c->ones.p, {o}), 0.0, gam, s);
+  einsum(2.0, "Qpq,Q->pq", Bt, gam, 1.0, F, s);
+  einsum(-1.0, "Qpk,Qkq->pq", slice(Bt, 2, 0, o), slice(Bt, 1, 0, o), 1.0, F, s);
+  TView Foo_ = blk(rm(c->F.p, {1, n, n}), 0, o, 0, o), Fov_ = blk(rm(c->F.p, {1, n, n}), 0, o, o, v);
+  TView Fvo_ = blk(rm(c->F.p, {1, n, n}), o, v, 0, o), Fvv_ = blk(rm(c->F.p, {1, n, n}), o, v, o, v);
+  auto drop0 = [](TView t) {  // remove the leading unit index
+    TView r; r.p = t.p; r.rank = t.rank - 1;
+    for (int k = 1; k < t.rank; ++k) { r.dim[k - 1] = t.dim[k]; r.str[k - 1] = t.str[k]; }
+    return r;
+  };
+  TView Foo = drop0(Foo_), Fov = drop0(Fov_), Fvo = drop0(Fvo_), Fvv = drop0(Fvv_);
+
+  TView ovov = rm(c->ovov.p, {o, v, o, v});
+  TView L = rm(c->Lldkc.p, {o, v, o, v});
+  TView u = rm(c->u.p, {o, o, v, v});
+  TView R2 = rm(c->r2.p, {o, o, v, v});
+  TView R1 = rm(c->r1.p, {o, v});
+  TView P = rm(c->P.p, {o, o, v, v});
+  TView Ci = rm(c->Cint.p, {o, o, v, v});   // [k][i][a][c]
+  TView Di = rm(c->Dint.p, {v, o, o, v});   // [a][i][k][c]
+  TView Xo = rm(c->Xo.p, {o, o, o, o});     // [k][i][l][j]
+
+  // u_ijab = 2 t_ijab - t_jiab
+  einsum1(2.0, "ijab->ijab", t2, 0.0, u, s);
+  einsum1(-1.0, "jiab->ijab", t2, 1.0, u, s);
+
+  // ---- doubles
+  einsum(1.0, "Qai,Qbj->ijab", Btvo, Btvo, 0.0, R2, s);                 // (ai|bj)
+  // particle-particle ladder, one block of virtual a at a time (no vvvv)
+  for (int64_t a0 = 0; a0 < v; a0 += c->ladder_block) {
+    int64_t na = std::min<int64_t>(c->ladder_block, v - a0);
+    TView W = rm(c->Wslab.p, {na, v, v, v});                               // [a][c][b][d]
+    einsum(1.0, "Qac,Qbd->acbd", slice(Btvv, 1, a0, na), Btvv, 0.0, W, s);
+    einsum(1.0, "ijcd,acbd->ijab", t2, W, 1.0, slice(R2, 2, a0, na), s);
+  }
+  // hole-hole ladder
+  einsum(1.0, "Qki,Qlj->kilj", Btoo, Btoo, 0.0, Xo, s);
+  einsum(1.0, "ijcd,kcld->kilj", t2, ovov, 1.0, Xo, s);
+  einsum(1.0, "klab,kilj->ijab", t2, Xo, 1.0, R2, s);
+  // C and D intermediates
+  einsum(1.0, "Qki,Qac->kiac", Btoo, Btvv, 0.0, Ci, s);                 // (ki|ac)
+  einsum(2.0, "Qai,Qkc->aikc", Btvo, Btov, 0.0, Di, s);                 // 2 (ai|kc)
+  einsum1(-1.0, "kiac->aikc", Ci, 1.0, Di, s);                          // - (ac|ki)
+  einsum(0.5, "ilad,ldkc->aikc", u, L, 1.0, Di, s);
+  einsum(-0.5, "liad,kdlc->kiac", t2, ovov, 1.0, Ci, s);
+  einsum(-0.5, "kjbc,kiac->ijab", t2, Ci, 0.0, P, s);
+  einsum(-1.0, "kibc,kjac->ijab", t2, Ci, 1.0, P, s);
+  einsum(0.5, "jkbc,aikc->ijab", u, Di, 1.0, P, s);
+  // Fock-like terms
+  TView Fvvp = rm(c->Fvv.p, {v, v}), Foop = rm(c->Foo.p, {o, o});
+  einsum1(1.0, "bc->bc", Fvv, 0.0, Fvvp, s);
+  TView V2 = rm(c->V2.p, {o, o, v, v});
+  einsum(-1.0, "klbd,klcd->bc", u, V2, 1.0, Fvvp, s);
+  einsum1(1.0, "kj->kj", Foo, 0.0, Foop, s);
+  einsum(1.0, "jlcd,klcd->kj", u, V2, 1.0, Foop, s);
+  einsum(1.0, "ijac,bc->ijab", t2, Fvvp, 1.0, P, s);
+  einsum(-1.0, "ikab,kj->ijab", t2, Foop, 1.0, P, s);
+  einsum1(1.0, "ijab->ijab", P, 1.0, R2, s);
+  einsum1(1.0, "jiba->ijab", P, 1.0, R2, s);
+
+  // ---- singles
+  einsum1(1.0, "ai->ia", Fvo, 0.0, R1, s);
+  TView Xq = rm(c->Xq.p, {Q, o, v}), Yq = rm(c->Yq.p, {Q, o, v});
+  einsum(1.0, "kicd,Qkc->Qid", u, Btov, 0.0, Xq, s);
+  einsum(1.0, "Qad,Qid->ia", Btvv, Xq, 1.0, R1, s);
+  einsum(1.0, "klac,Qlc->Qka", u, Btov, 0.0, Yq, s);
+  einsum(-1.0, "Qki,Qka->ia", Btoo, Yq, 1.0, R1, s);
+  einsum(1.0, "ikac,kc->ia", u, Fov, 1.0, R1, s);
+}
+
+// --------------------------------------------------------------- iteration
+namespace {
+
+struct DiisState {
+  int ndiis = 0;
+  bool fp32 = true;
+  int64_t len = 0;
+  std::vector<int> valid;          // slot -> 1 if occupied
+  std::vector<double> norm2;       // ||e_k||^2 in stored precision
+  std::vector<std::vector<double>> dot;  // dot[i][j]
+  std::vector<int> age;            // insertion order, for a stable ordering of the subspace
+  int counter = 0;
+  int count() const { int n = 0; for (int x : valid) n += x; return n; }
+};
+
+double* vec_slot(DBuf<double>& vecs, int64_t len, int k) { return vecs.p + (int64_t)k * len; }
+
+}  // namespace
+
+int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_cap, fcc_ccsd_result* res) {
+  cudaStream_t s = c->stream;
+  const int64_t o = c->o, v = c->v;
+  const int64_t len1 = o * v, len2 = o * o * v * v;
+  fcc_opts op = *opt;
+  if (op.max_iter < 0 || op.ndiis < 1 || op.ndiis > MAX_DIIS || op.diis_relax < 1 || op.damp < 0 || op.damp >= 1)
+    fail(FCC_ERR_BAD_ARG, "invalid CC options");
+  if (op.precision != FCC_PREC_FP64)
+    fail(FCC_ERR_BAD_ARG, "this build runs FCC_PREC_FP64 only");
+  bool diis = op.diis != 0;
+  bool fp32err = op.diis_prec != 64;
+
+  // amplitude buffers: "cur" = newT of the reference loop
+  DBuf<double> tn1, tn2, tx1, tx2;
+  tn1.alloc(len1); tn2.alloc(len2);
+  DiisState D1s, D2s;
+  if (diis) {
+    c->dvec1.alloc(len1 * op.ndiis);
+    c->dvec2.alloc(len2 * op.ndiis);
+    if (fp32err) { c->derr1s.alloc(len1 * op.ndiis); c->derr2s.alloc(len2 * op.ndiis); }
+    else { c->derr1d.alloc(len1 * op.ndiis); c->derr2d.alloc(len2 * op.ndiis); }
+    tx1.alloc(len1); tx2.alloc(len2);
+    for (auto* d : {&D1s, &D2s}) {
+      d->ndiis = op.ndiis; d->fp32 = fp32err;
+      d->valid.assign(op.ndiis, 0); d->norm2.assign(op.ndiis, 0.0);
+      d->dot.assign(op.ndiis, std::vector<double>(op.ndiis, 0.0)); d->age.assign(op.ndiis, 0);
+    }
+    D1s.len = len1; D2s.len = len2;
+  }
+  // newT starts as the guess held in c->t1/c->t2
+  FCC_CUDA(cudaMemcpyAsync(tn1.p, c->t1.p, sizeof(double) * len1, cudaMemcpyDeviceToDevice, s));
+  FCC_CUDA(cudaMemcpyAsync(tn2.p, c->t2.p, sizeof(double) * len2, cudaMemcpyDeviceToDevice, s));
+  double* cur1 = tn1.p;
+  double* cur2 = tn2.p;
+
+  double Ecc = cc_energy(c, cur1, cur2);                                   // RCCSDa.jl:168
+  double Eguess = Ecc + c->e_ref;
+  double dE = 1.0, rms = 1.0;
+  int ite = 1, nlog = 0;
+  double* hred = nullptr;
+  FCC_CUDA(cudaMallocHost(&hred, sizeof(double) * 64));
+  struct HostFree { double* p; ~HostFree() { if (p) cudaFreeHost(p); } } hf{hred};
+  DBuf<double> dB, dcoef;
+  DBuf<int> dstat;
+  dB.alloc((MAX_DIIS + 1) * (MAX_DIIS + 1));
+  dcoef.alloc(MAX_DIIS + 1);
+  dstat.alloc(4);
+  cudaEvent_t ev0, ev1;
+  FCC_CUDA(cudaEventCreate(&ev0));
+  FCC_CUDA(cudaEventCreate(&ev1));
+  struct EvFree { cudaEvent_t a, b; ~EvFree() { cudaEventDestroy(a); cudaEventDestroy(b); } } evf{ev0, ev1};
+  double* dout = c->red.p + RED_BLOCKS * NPART;
+
+  auto run_update = [&](int rank, DiisState& ds, DBuf<double>& vecs, DBuf<float>& es, DBuf<double>& ed,
+                        const double* T, const double* R, DBuf<double>& plain, double** cur, const double* t1new,
+                        double* out_sumsq, double* out_energy) {
+    int64_t len = rank == 2 ? len1 : len2;
+    ErrSlots others{};
+    int target = -1;
+    std::vector<int> other_ids;
+    if (diis) {
+      // DIIS.jl:38-50: evict the slot with the largest error norm when full
+      if (ds.count() + 1 > ds.ndiis) {
+        int worst = -1;
+        for (int k = 0; k < ds.ndiis; ++k)
+          if (ds.valid[k] && (worst < 0 || ds.norm2[k] > ds.norm2[worst])) worst = k;
+        ds.valid[worst] = 0;
+        target = worst;
+      } else {
+        for (int k = 0; k < ds.ndiis; ++k) if (!ds.valid[k]) { target = k; break; }
+      }
+      for (int k = 0; k < ds.ndiis; ++k)
+        if (ds.valid[k]) {
+          others.s[others.n] = ds.fp32 ? es.p + (int64_t)k * len : nullptr;
+          others.d[others.n] = ds.fp32 ? nullptr : ed.p + (int64_t)k * len;
+          other_ids.push_back(k);
+          others.n++;
+        }
+    }
+    double* dst = diis ? vec_slot(vecs, len, target) : plain.p;
+    float* errs = (diis && ds.fp32) ? es.p + (int64_t)target * len : nullptr;
+    double* errd = (diis && !ds.fp32) ? ed.p + (int64_t)target * len : nullptr;
+    update_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(rank, T, R, c->eps.p, (int)o, (int)v, dst, errs, errd, others,
+                                                     rank == 4 ? c->Lt.p : nullptr, t1new, c->red.p);
+    FCC_CHECK_LAUNCH();
+    finish_reduce_kernel<<<1, 32, 0, s>>>(c->red.p, RED_BLOCKS, 2 + others.n, dout);
+    FCC_CHECK_LAUNCH();
+    int nself = 0;
+    if (diis) {
+      selfdot_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(len, errs, errd, c->red.p);
+      FCC_CHECK_LAUNCH();
+      finish_reduce_kernel<<<1, 32, 0, s>>>(c->red.p, RED_BLOCKS, 1, dout + 2 + MAX_DIIS);
+      FCC_CHECK_LAUNCH();
+      nself = 1;
+    }
+    FCC_CUDA(cudaMemcpyAsync(hred, dout, sizeof(double) * (2 + MAX_DIIS + nself), cudaMemcpyDeviceToHost, s));
+    FCC_CUDA(cudaStreamSynchronize(s));
+    *out_sumsq = hred[0];
+    *out_energy = hred[1];
+    if (diis) {
+      ds.valid[target] = 1;
+      ds.age[target] = ++ds.counter;
+      ds.norm2[target] = hred[2 + MAX_DIIS];
+      ds.dot[target][target] = hred[2 + MAX_DIIS];
+      for (size_t q = 0; q < other_ids.size(); ++q) {
+        ds.dot[target][other_ids[q]] = hred[2 + q];
+        ds.dot[other_ids[q]][target] = hred[2 + q];
+      }
+    }
+    *cur = dst;
+  };
+
+  auto extrapolate = [&](int rank, DiisState& ds, DBuf<double>& vecs, DBuf<float>& es, DBuf<double>& ed,
+                         DBuf<double>& outbuf, const double* t1new, double* out_energy) -> bool {
+    int64_t len = rank == 2 ? len1 : len2;
+    std::vector<int> ids;
+    for (int k = 0; k < ds.ndiis; ++k) if (ds.valid[k]) ids.push_back(k);
+    std::sort(ids.begin(), ids.end(), [&](int a, int b) { return ds.age[a] < ds.age[b]; });
+    int m = (int)ids.size();
+    if (m < 2) fail(FCC_ERR_STATE, "DIIS cannot extrapolate from one vector");
+    int N = m + 1;
+    std::vector<double> Bm(N * N, 1.0);
+    Bm[N * N - 1] = 0.0;
+    for (int a = 0; a < m; ++a)
+      for (int b = 0; b < m; ++b) Bm[a * N + b] = ds.dot[ids[a]][ids[b]];
+    FCC_CUDA(cudaMemcpyAsync(dB.p, Bm.data(), sizeof(double) * N * N, cudaMemcpyHostToDevice, s));
+    diis_solve_kernel<<<1, 1, 0, s>>>(dB.p, N, dcoef.p, dstat.p);
+    FCC_CHECK_LAUNCH();
+    VecSlots sl{};
+    for (int a = 0; a < m; ++a) {
+      sl.vec[a] = vec_slot(vecs, len, ids[a]);
+      sl.es[a] = ds.fp32 ? es.p + (int64_t)ids[a] * len : nullptr;
+      sl.ed[a] = ds.fp32 ? nullptr : ed.p + (int64_t)ids[a] * len;
+    }
+    sl.n = m;
+    extrapolate_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(rank, (int)o, (int)v, sl, dcoef.p, outbuf.p,
+                                                          rank == 4 ? c->Lt.p : nullptr, t1new, c->red.p);
+    FCC_CHECK_LAUNCH();
+    finish_reduce_kernel<<<1, 32, 0, s>>>(c->red.p, RED_BLOCKS, 2, dout);
+    FCC_CHECK_LAUNCH();
+    int st = 0;
+    FCC_CUDA(cudaMemcpyAsync(hred, dout, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+    FCC_CUDA(cudaMemcpyAsync(&st, dstat.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FCC_CUDA(cudaStreamSynchronize(s));
+    if (st) fail(FCC_ERR_NAN, "singular DIIS matrix");
+    *out_energy = hred[1];
+    return true;
+  };
+
+  int status = FCC_OK;
+  while (std::fabs(dE) > op.e_conv || rms > op.max_rms) {                   // RCCSDa.jl:178
+    if (ite > op.max_iter) { status = FCC_NO_CONVERGE; break; }            // :179-182
+    FCC_CUDA(cudaEventRecord(ev0, s));
+    // T1 .= newT1; T2 .= newT2                                              // :185-186
+    if (cur1 != c->t1.p) FCC_CUDA(cudaMemcpyAsync(c->t1.p, cur1, sizeof(double) * len1, cudaMemcpyDeviceToDevice, s));
+    if (cur2 != c->t2.p) FCC_CUDA(cudaMemcpyAsync(c->t2.p, cur2, sizeof(double) * len2, cudaMemcpyDeviceToDevice, s));
+    double oldE = Ecc;
+    residual_fp64(c);                                                      // :190
+    double ss1, ss2, e_dummy, e_new;
+    run_update(2, D1s, c->dvec1, c->derr1s, c->derr1d, c->t1.p, c->r1.p, tn1, &cur1, nullptr, &ss1, &e_dummy);
+    run_update(4, D2s, c->dvec2, c->derr2s, c->derr2d, c->t2.p, c->r2.p, tn2, &cur2, cur1, &ss2, &e_new);
+    double r1 = std::sqrt(ss1 / (double)len1), r2 = std::sqrt(ss2 / (double)len2);   // :193-194
+    bool did = false;
+    if (diis && ite >= op.diis_start && ite % op.diis_relax == 0) {        // :204
+      double e1d;
+      extrapolate(2, D1s, c->dvec1, c->derr1s, c->derr1d, tx1, nullptr, &e1d);
+      extrapolate(4, D2s, c->dvec2, c->derr2s, c->derr2d, tx2, tx1.p, &e_new);
+      cur1 = tx1.p;
+      cur2 = tx2.p;
+      did = true;
+    }
+    if (op.damp > 0) {                                                     // :213-216
+      double dp = op.damp;
+      double* d1 = (cur1 == tx1.p) ? tx1.p : tn1.p;
+      double* d2 = (cur2 == tx2.p) ? tx2.p : tn2.p;
+      if (cur1 != d1) FCC_CUDA(cudaMemcpyAsync(d1, cur1, sizeof(double) * len1, cudaMemcpyDeviceToDevice, s));
+      if (cur2 != d2) FCC_CUDA(cudaMemcpyAsync(d2, cur2, sizeof(double) * len2, cudaMemcpyDeviceToDevice, s));
+      axpby_flat_kernel<<<grid_for(len1), 256, 0, s>>>(d1, c->t1.p, len1, 1 - dp, dp);
+      axpby_flat_kernel<<<grid_for(len2), 256, 0, s>>>(d2, c->t2.p, len2, 1 - dp, dp);
+      FCC_CHECK_LAUNCH();
+      cur1 = d1;
+      cur2 = d2;
+      e_new = cc_energy(c, cur1, cur2);
+    }
+    Ecc = e_new;                                                           // :218
+    rms = std::max(r1, r2);                                                // :220
+    dE = Ecc - oldE;                                                       // :221
+    FCC_CUDA(cudaEventRecord(ev1, s));
+    FCC_CUDA(cudaEventSynchronize(ev1));
+    float ms = 0;
+    FCC_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+    if (!std::isfinite(Ecc) || !std::isfinite(rms)) { status = FCC_ERR_NAN; }
+    if (log && nlog < log_cap) {
+      fcc_iter_stats& L = log[nlog];
+      L.ite = ite; L.diis = did; L.precision = FCC_PREC_FP64; L.pad = 0;
+      L.energy = Ecc; L.dE = dE; L.rms = rms; L.seconds = ms * 1e-3;
+    }
+    ++nlog;
+    ++ite;
+    if (status == FCC_ERR_NAN) break;
+  }
+  // keep the final amplitudes in c->t1 / c->t2
+  if (cur1 != c->t1.p) FCC_CUDA(cudaMemcpyAsync(c->t1.p, cur1, sizeof(double) * len1, cudaMemcpyDeviceToDevice, s));
+  if (cur2 != c->t2.p) FCC_CUDA(cudaMemcpyAsync(c->t2.p, cur2, sizeof(double) * len2, cudaMemcpyDeviceToDevice, s));
+  FCC_CUDA(cudaStreamSynchronize(s));
+  c->dvec1.release(); c->dvec2.release(); c->derr1s.release(); c->derr2s.release();
+  c->derr1d.release(); c->derr2d.release();
+  if (res) {
+    res->guessenergy = Eguess;
+    res->correlation = Ecc;
+    res->energy = Ecc + c->e_ref;
+    res->e_conv = dE;
+    res->t_conv = rms;
+    res->iterations = nlog;
+    res->converged = (std::fabs(dE) < op.e_conv && rms < op.max_rms) ? 1 : 0;   // :231
+  }
+  c->have_ccsd = true;
+  return status;
+}
+
+}  // namespace fcc

@@ -1,0 +1,123 @@
+// Shared definitions for the GB300 coupled-cluster library (libfermicc).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/fermicc.h"
+
+namespace fcc {
+
+// Internal exception carrying an fcc status code; converted to a return code
+// at the C ABI so nothing ever aborts the caller's process.
+struct Error {
+  int code;
+  std::string what;
+};
+
+[[noreturn]] inline void fail(int code, const std::string& what) { throw Error{code, what}; }
+
+#define FCC_CUDA(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e__ = (call);                                                                   \
+    if (e__ != cudaSuccess)                                                                     \
+      ::fcc::fail(e__ == cudaErrorMemoryAllocation ? FCC_ERR_OOM : FCC_ERR_CUDA,                \
+                  std::string(#call) + ": " + cudaGetErrorString(e__));                         \
+  } while (0)
+
+#define FCC_CHECK_LAUNCH() FCC_CUDA(cudaGetLastError())
+
+// Device buffer owned by a context.
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    if (count == 0) return;
+    FCC_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void zero(cudaStream_t s) { if (p) FCC_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s)); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// A strided view of a device tensor with up to 4 named indices.
+struct TView {
+  double* p = nullptr;
+  int rank = 0;
+  int64_t dim[4] = {1, 1, 1, 1};
+  int64_t str[4] = {0, 0, 0, 0};
+};
+
+// Row-major view (last index fastest) over a contiguous buffer.
+inline TView rm(double* p, std::initializer_list<int64_t> dims) {
+  TView t;
+  t.p = p;
+  t.rank = (int)dims.size();
+  int k = 0;
+  for (auto d : dims) t.dim[k++] = d;
+  int64_t s = 1;
+  for (int i = t.rank - 1; i >= 0; --i) { t.str[i] = s; s *= t.dim[i]; }
+  return t;
+}
+// Column-major view (first index fastest), the layout of Julia arrays.
+inline TView cm(double* p, std::initializer_list<int64_t> dims) {
+  TView t;
+  t.p = p;
+  t.rank = (int)dims.size();
+  int k = 0;
+  for (auto d : dims) t.dim[k++] = d;
+  int64_t s = 1;
+  for (int i = 0; i < t.rank; ++i) { t.str[i] = s; s *= t.dim[i]; }
+  return t;
+}
+// Sub-range of one index (offsets the pointer, shrinks the extent).
+inline TView slice(TView t, int idx, int64_t begin, int64_t count) {
+  t.p += begin * t.str[idx];
+  t.dim[idx] = count;
+  return t;
+}
+
+// ---------------------------------------------------------------- kernels
+// Contraction descriptor consumed by the FP64 kernel: M = M1*M2, N = N1*N2,
+// K = K1*K2 with independent strides for every sub-index, plus a batch
+// index with uniform strides.
+struct CtrDesc {
+  int64_t M, N, K, M2, N2, K2, batch;
+  int64_t a_m1, a_m2, a_k1, a_k2, a_b;
+  int64_t b_k1, b_k2, b_n1, b_n2, b_b;
+  int64_t c_m1, c_m2, c_n1, c_n2, c_b;
+  double alpha, beta;
+};
+
+void contract_f64_launch(const double* A, const double* B, double* C, const CtrDesc& d, cudaStream_t s);
+
+// out[perm] = alpha * in + beta * out over a 4-index box (general strides).
+void tensor_axpby_launch(const TView& in, const TView& out, double alpha, double beta, cudaStream_t s);
+
+// Einsum front end: C = alpha * contract(A, B) + beta * C.  Subscripts use
+// single letters; every index of C must appear in A or B.  Indices are
+// grouped into batch (A,B,C), M (A,C), N (B,C) and K (A,B); each group may
+// hold at most two indices (batch at most one).
+void einsum(double alpha, const char* spec, const TView& A, const TView& B, double beta, const TView& C,
+            cudaStream_t s);
+// Single-operand form "abcd->dcba": C = alpha * permute(A) + beta * C.
+void einsum1(double alpha, const char* spec, const TView& A, double beta, const TView& C, cudaStream_t s);
+
+}  // namespace fcc

@@ -1,0 +1,53 @@
+// Context of one coupled-cluster problem on one GPU: device tensors, stream,
+// options and the iteration state.
+#pragma once
+#include "fcc_common.cuh"
+
+struct fcc_ctx {
+  int device = 0;
+  int64_t o = 0, v = 0, Q = 0, n = 0;
+  double e_ref = 0.0;
+  bool have_ints = false, have_guess = false, have_ccsd = false;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  std::vector<double> eps_h;  // o + v orbital energies (host copy)
+
+  // three-index factors, full MO range (active occupied + virtual):
+  //   B[Q][p][q] row-major (q fastest), undressed and T1-dressed
+  fcc::DBuf<double> B, Bt;
+  fcc::DBuf<double> eps;      // o + v
+  fcc::DBuf<double> h;        // n x n: diag(eps) - G(B), the frozen-core-including one-body part
+  fcc::DBuf<double> F;        // n x n dressed Fock
+  fcc::DBuf<double> Xm, Ym, tmpnn;
+  fcc::DBuf<double> ones;     // length max(o, Q)
+  fcc::DBuf<double> gam;      // Q
+  // constant integrals
+  fcc::DBuf<double> ovov;     // (kc|ld)      [o][v][o][v]
+  fcc::DBuf<double> Lldkc;    // 2(ld|kc)-(lc|kd)  [o][v][o][v]
+  fcc::DBuf<double> Lt;       // 2(kc|ld)-(kd|lc)  [o][o][v][v] (energy)
+  fcc::DBuf<double> V2;       // (kc|ld)           [k][l][c][d]
+  // amplitudes and residuals
+  fcc::DBuf<double> t1, t2;   // current amplitudes [o][v], [o][o][v][v]
+  fcc::DBuf<double> r1, r2;   // residuals
+  fcc::DBuf<double> u, P, Cint, Dint, Xo, Wslab, Xq, Yq, Fvv, Foo;
+  // reductions
+  fcc::DBuf<double> red;      // device scratch for scalar reductions
+  int64_t ladder_block = 0;
+
+  // DIIS storage (slots of vec + err for T1 and T2)
+  fcc::DBuf<double> dvec1, dvec2;
+  fcc::DBuf<float> derr1s, derr2s;
+  fcc::DBuf<double> derr1d, derr2d;
+
+  // (T) scratch
+  fcc::DBuf<double> ovvv, ooov, Wt;
+};
+
+namespace fcc {
+void setup_integrals(fcc_ctx* c);
+void make_mp2_guess(fcc_ctx* c);
+double cc_energy(fcc_ctx* c, const double* t1, const double* t2);
+void residual_fp64(fcc_ctx* c);
+int ccsd_run(fcc_ctx* c, const fcc_opts* opts, fcc_iter_stats* log, int32_t log_cap, fcc_ccsd_result* out);
+double triples_fp64(fcc_ctx* c);
+}  // namespace fcc

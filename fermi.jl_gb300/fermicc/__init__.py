@@ -1,0 +1,13 @@
+"""GB300 backend for Fermi.jl's RCCSD / DF-RCCSD / RCCSD(T) path.
+
+Compute runs in hand-written sm_103a CUDA kernels behind the C ABI of
+``libfermicc.so`` (include/fermicc.h); this package is the host-side mirror of
+Fermi's method objects and options, plus the stand-in input pipeline
+(``fermicc.inputs``) that produces the integrals Fermi would hand over.
+"""
+from . import options as Options
+from .options import FermiException
+from .rccsd import CudaPT, RCCSD, RCCSDcuda, RCCSDpT, energy, get_pt_alg, get_rccsd_alg
+
+__all__ = ["Options", "FermiException", "RCCSD", "RCCSDpT", "RCCSDcuda", "CudaPT", "energy",
+           "get_rccsd_alg", "get_pt_alg"]

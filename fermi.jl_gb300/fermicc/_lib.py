@@ -1,0 +1,86 @@
+"""ctypes binding of libfermicc.so (the C ABI declared in include/fermicc.h).
+
+The library is looked up next to the package (built in-tree by build.py).  A
+missing library is an error: there is no CPU fallback for the
+coupled-cluster path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(HERE), "libfermicc.so")
+
+FCC_OK = 0
+FCC_ERR_BAD_ARG = -1
+FCC_ERR_OOM = -2
+FCC_ERR_CUDA = -3
+FCC_NO_CONVERGE = -4
+FCC_ERR_NAN = -5
+FCC_ERR_TIMEOUT = -6
+FCC_ERR_STATE = -7
+FCC_ERR_NO_DEVICE = -8
+FCC_PREC_FP64 = 0
+FCC_PREC_MIXED = 1
+
+# every symbol the header declares
+EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess",
+           "fcc_ccsd_run", "fcc_get_amps", "fcc_triples", "fcc_destroy", "fcc_strerror", "fcc_last_error")
+
+
+class FccOpts(ctypes.Structure):
+    _fields_ = [("max_iter", ctypes.c_int32), ("diis", ctypes.c_int32), ("ndiis", ctypes.c_int32),
+                ("diis_start", ctypes.c_int32), ("diis_relax", ctypes.c_int32), ("diis_prec", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32), ("e_conv", ctypes.c_double),
+                ("max_rms", ctypes.c_double), ("damp", ctypes.c_double), ("mixed_switch_rms", ctypes.c_double)]
+
+
+class FccIterStats(ctypes.Structure):
+    _fields_ = [("ite", ctypes.c_int32), ("diis", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("energy", ctypes.c_double), ("dE", ctypes.c_double),
+                ("rms", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+
+class FccCCSDResult(ctypes.Structure):
+    _fields_ = [("guessenergy", ctypes.c_double), ("correlation", ctypes.c_double), ("energy", ctypes.c_double),
+                ("e_conv", ctypes.c_double), ("t_conv", ctypes.c_double), ("iterations", ctypes.c_int32),
+                ("converged", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def load():
+    """Load libfermicc.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libfermicc.so not found at {LIB_PATH}: run __graft_entry__.build() "
+                           "(the coupled-cluster path has no CPU fallback)")
+    lib = ctypes.CDLL(LIB_PATH)
+    dp = ctypes.POINTER(ctypes.c_double)
+    vp = ctypes.c_void_p
+    i32 = ctypes.c_int32
+    lib.fcc_default_opts.argtypes = [ctypes.POINTER(FccOpts)]
+    lib.fcc_default_opts.restype = None
+    lib.fcc_create.argtypes = [ctypes.POINTER(vp), i32, i32, i32, i32]
+    lib.fcc_upload_df.argtypes = [vp, dp, dp, dp, dp, dp, ctypes.c_double]
+    lib.fcc_upload_conv.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, dp, ctypes.c_double]
+    lib.fcc_set_guess.argtypes = [vp, dp, dp]
+    lib.fcc_ccsd_run.argtypes = [vp, ctypes.POINTER(FccOpts), ctypes.POINTER(FccIterStats), i32,
+                                 ctypes.POINTER(FccCCSDResult)]
+    lib.fcc_get_amps.argtypes = [vp, dp, dp]
+    lib.fcc_triples.argtypes = [vp, i32, dp]
+    lib.fcc_destroy.argtypes = [vp]
+    lib.fcc_destroy.restype = None
+    lib.fcc_strerror.argtypes = [ctypes.c_int]
+    lib.fcc_strerror.restype = ctypes.c_char_p
+    lib.fcc_last_error.argtypes = [vp]
+    lib.fcc_last_error.restype = ctypes.c_char_p
+    for name in ("fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess", "fcc_ccsd_run",
+                 "fcc_get_amps", "fcc_triples"):
+        getattr(lib, name).restype = ctypes.c_int
+    _lib = lib
+    return lib

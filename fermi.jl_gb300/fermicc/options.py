@@ -1,0 +1,93 @@
+"""Options for the coupled-cluster backend, mirroring ``Fermi.Options``.
+
+Fermi keeps global option dictionaries (``Default`` / ``Current``), lower-cases
+keys, rejects unknown keys and coerces values to the default's type
+(src/Core/Options.jl:40-189); failures raise ``FermiException``
+(src/Core/Options.jl:196-199).  This module keeps the same behaviour for the
+keys the coupled-cluster path reads, plus the keys this backend adds:
+
+* ``cc_alg``  -- 2 selects this backend (``RCCSDcuda``); Fermi's 1 is its Julia
+  ``RCCSDa`` and is not provided here.
+* ``pt_alg``  -- 4 selects this backend's (T) (``CudaPT``); Fermi's 1-3 are its
+  Julia ``ijk`` / ``ijk2`` / ``abc``.
+* ``cc_gpu_precision`` -- "fp64" or "mixed" (split-BF16 contractions with an
+  FP64 finish).
+* ``cc_gpu_switch_rms`` -- residual at which the mixed form switches to FP64.
+* ``cc_gpu_guess`` -- "mp2" or "mlp" (learned T2 initialiser).
+* ``pt_gpu_precision`` -- "fp64" or "mixed" for (T).
+"""
+from __future__ import annotations
+
+
+class FermiException(Exception):
+    """Same role as ``Fermi.Options.FermiException``."""
+
+
+DEFAULT = {
+    "cc_alg": 2,
+    "pt_alg": 4,
+    "cc_max_iter": 50,
+    "cc_max_rms": 1e-10,
+    "cc_e_conv": 1e-10,
+    "cc_diis": True,
+    "cc_ndiis": 3,
+    "cc_diis_relax": 3,
+    "diis_start": 3,
+    "diis_prec": "single",
+    "cc_damp_ratio": 0.0,
+    "drop_occ": 0,
+    "drop_vir": 0,
+    "df": True,
+    "return_ints": False,
+    "precision": "double",
+    "cc_gpu_precision": "fp64",
+    "cc_gpu_switch_rms": 1e-5,
+    "cc_gpu_guess": "mp2",
+    "pt_gpu_precision": "fp64",
+    "cc_gpu_device": 0,
+}
+
+_current: dict = {}
+
+
+def _coerce(key: str, val):
+    ref = DEFAULT[key]
+    try:
+        if isinstance(ref, bool):
+            if isinstance(val, str):
+                if val.lower() in ("true", "false"):
+                    return val.lower() == "true"
+                raise ValueError
+            return bool(val)
+        if isinstance(ref, int):
+            if isinstance(val, float) and not val.is_integer():
+                raise ValueError
+            return int(val)
+        if isinstance(ref, float):
+            return float(val)
+        if isinstance(ref, str):
+            return str(val).lower()
+    except (TypeError, ValueError):
+        pass
+    raise FermiException(f"invalid type for option {key}: {val!r}")
+
+
+def set(key: str, val) -> None:  # noqa: A001 - mirrors Fermi.Options.set
+    k = key.lower()
+    if k not in DEFAULT:
+        raise FermiException(f"invalid option: {key}")
+    _current[k] = _coerce(k, val)
+
+
+def get(key: str):
+    k = key.lower()
+    if k not in DEFAULT:
+        raise FermiException(f"invalid option: {key}")
+    return _current.get(k, DEFAULT[k])
+
+
+def reset(key: str | None = None) -> None:
+    if key is None:
+        _current.clear()
+    else:
+        _current.pop(key.lower(), None)

@@ -1,0 +1,137 @@
+/*
+ * fermicc.h -- C ABI of the GB300 coupled-cluster backend (libfermicc.so).
+ *
+ * This is the drop-in boundary for Fermi.jl's RCCSD / DF-RCCSD amplitude
+ * iteration and RCCSD(T) correction.  Every entry point takes plain pointers
+ * and sizes, returns an int status (0 = success, negative = error) and never
+ * aborts the caller.  Arrays are COLUMN-MAJOR (Julia layout): the first index
+ * is the fastest.  The library copies every input to the device during the
+ * call and keeps no host pointer afterwards.
+ *
+ * Reference interfaces replaced (paths inside FermiQC/Fermi.jl v0.5.0):
+ *   fcc_create / fcc_upload_df     RCCSD(moints, aoints, ::RCCSDa), DF overload,
+ *                                  src/Methods/CoupledCluster/RCCSD/RCCSDa.jl:37-44
+ *                                  (moints["BOO"], ["BOV"], ["BVV"], ["Fd"])
+ *   fcc_upload_conv                the conventional overload, RCCSDa.jl:25-35
+ *                                  (moints["OOOO"] .. ["VVVV"])
+ *   fcc_set_guess                  RCCSD(moints, T1guess, T2guess, alg), RCCSDa.jl:92
+ *                                  (without it: the MP2 guess of RCCSDa.jl:46-89)
+ *   fcc_ccsd_run                   the iteration loop, RCCSDa.jl:92-244, with the
+ *                                  equations of RCCSDHelper.jl:8-349 and DIIS.jl
+ *   fcc_get_amps                   the T1 / T2 fields of struct RCCSD, RCCSD.jl:61-69
+ *   fcc_triples                    RCCSDpT(ccsd, moints, ::ijk),
+ *                                  src/Methods/CoupledCluster/PerturbativeTriples/ijk.jl:20-149
+ *   fcc_strerror                   FermiException messages, src/Core/Options.jl:196-199
+ */
+#ifndef FERMICC_H
+#define FERMICC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FCC_OK 0
+#define FCC_ERR_BAD_ARG (-1)   /* invalid size, null pointer, bad option        */
+#define FCC_ERR_OOM (-2)       /* device allocation failed                       */
+#define FCC_ERR_CUDA (-3)      /* CUDA runtime error                             */
+#define FCC_NO_CONVERGE (-4)   /* soft: max_iter reached, results still valid    */
+#define FCC_ERR_NAN (-5)       /* non-finite amplitudes or energy detected       */
+#define FCC_ERR_TIMEOUT (-6)   /* a bounded device wait gave up                  */
+#define FCC_ERR_STATE (-7)     /* call out of order (e.g. triples before ccsd)   */
+#define FCC_ERR_NO_DEVICE (-8) /* no usable sm_103 device                        */
+
+/* arithmetic of the contractions */
+#define FCC_PREC_FP64 0  /* FP64 throughout (the correctness form)                  */
+#define FCC_PREC_MIXED 1 /* split-BF16 tensor-core contractions, FP32 accumulate,   */
+                         /* FP64 denominators/update/DIIS/energies, FP64 finish    */
+
+typedef struct fcc_ctx fcc_ctx;
+
+/* Fermi's CC options (src/Core/Options.jl:40-104) plus the precision switch. */
+typedef struct {
+  int32_t max_iter;        /* cc_max_iter    (50)                              */
+  int32_t diis;            /* cc_diis        (1)                               */
+  int32_t ndiis;           /* cc_ndiis       (3)                               */
+  int32_t diis_start;      /* diis_start     (3)                               */
+  int32_t diis_relax;      /* cc_diis_relax  (3)                               */
+  int32_t diis_prec;       /* diis_prec: 32 = "single" (default), 64 = "double" */
+  int32_t precision;       /* FCC_PREC_FP64 (default) or FCC_PREC_MIXED        */
+  int32_t reserved;
+  double e_conv;           /* cc_e_conv      (1e-10)                           */
+  double max_rms;          /* cc_max_rms     (1e-10)                           */
+  double damp;             /* cc_damp_ratio  (0.0)                             */
+  double mixed_switch_rms; /* mixed form: FP64 once rms < this (1e-5)          */
+} fcc_opts;
+
+/* One line of Fermi's iteration table (RCCSDa.jl:223). */
+typedef struct {
+  int32_t ite;
+  int32_t diis;      /* 1 if this iteration extrapolated                */
+  int32_t precision; /* FCC_PREC_* used for this iteration's residual   */
+  int32_t pad;
+  double energy;     /* correlation energy after the iteration          */
+  double dE;
+  double rms;        /* max(rms(dT1), rms(dT2))                         */
+  double seconds;    /* device time of the iteration                    */
+} fcc_iter_stats;
+
+/* Fields of struct RCCSD (RCCSD.jl:61-69) except the amplitudes. */
+typedef struct {
+  double guessenergy; /* Eguess = E_cc(guess) + E_ref                   */
+  double correlation; /* E_cc                                           */
+  double energy;      /* E_cc + E_ref                                   */
+  double e_conv;      /* last dE                                        */
+  double t_conv;      /* last rms                                       */
+  int32_t iterations;
+  int32_t converged;
+} fcc_ccsd_result;
+
+void fcc_default_opts(fcc_opts* opts);
+
+/* o active occupied, v active virtual, naux fitting functions (0 selects the
+ * conventional path, which then needs fcc_upload_conv).  device = CUDA
+ * ordinal; the device must be sm_103 (GB300). */
+int fcc_create(fcc_ctx** out, int32_t o, int32_t v, int32_t naux, int32_t device);
+
+/* Boo[Q,i,j] (naux x o x o), Bov[Q,i,a] (naux x o x v), Bvv[Q,a,b]
+ * (naux x v x v), all column-major with Q fastest, frozen core already
+ * removed; eps_o (o), eps_v (v) RHF orbital energies; e_ref the SCF energy. */
+int fcc_upload_df(fcc_ctx* ctx, const double* Boo, const double* Bov, const double* Bvv,
+                  const double* eps_o, const double* eps_v, double e_ref);
+
+/* Conventional MO blocks in chemist's notation, column-major:
+ * OOOO[i,j,k,l] = (ij|kl), OOOV[i,j,k,a], OOVV[i,j,a,b], OVOV[i,a,j,b],
+ * OVVV[i,a,b,c], VVVV[a,b,c,d].  Intended for small molecules. */
+int fcc_upload_conv(fcc_ctx* ctx, const double* OOOO, const double* OOOV, const double* OOVV,
+                    const double* OVOV, const double* OVVV, const double* VVVV,
+                    const double* eps_o, const double* eps_v, double e_ref);
+
+/* Starting amplitudes T1[i,a] (o x v) and T2[i,j,a,b] (o x o x v x v).
+ * Without this call the run starts from the MP2 guess. */
+int fcc_set_guess(fcc_ctx* ctx, const double* T1, const double* T2);
+
+/* Run the CCSD iterations.  log may be NULL; otherwise up to log_cap lines are
+ * written (one per iteration).  Returns FCC_NO_CONVERGE (with valid results)
+ * when max_iter is reached. */
+int fcc_ccsd_run(fcc_ctx* ctx, const fcc_opts* opts, fcc_iter_stats* log, int32_t log_cap,
+                 fcc_ccsd_result* out);
+
+/* Copy the current amplitudes to the host (either pointer may be NULL). */
+int fcc_get_amps(fcc_ctx* ctx, double* T1, double* T2);
+
+/* (T) correction from the converged amplitudes (FCC_PREC_FP64 or
+ * FCC_PREC_MIXED); et_out receives E(T). */
+int fcc_triples(fcc_ctx* ctx, int32_t precision, double* et_out);
+
+void fcc_destroy(fcc_ctx* ctx);
+const char* fcc_strerror(int code);
+/* Message of the last failing call on this context ("" if none). */
+const char* fcc_last_error(const fcc_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FERMICC_H */
