@@ -12,6 +12,7 @@
 #include <map>
 
 #include "fcc_common.cuh"
+#include "fcc_tc.cuh"
 
 namespace fcc {
 
@@ -242,7 +243,7 @@ void parse(const char* spec, std::vector<std::string>& ins, std::string& out) {
 
 // Fuse indices of a group until it has at most `cap` members; two indices x
 // (slower) and y (faster) fuse when str[x] == dim[y] * str[y] in every operand.
-void fuse(std::vector<Ix>& g, int cap, const char* spec) {
+bool try_fuse(std::vector<Ix>& g, int cap) {
   while ((int)g.size() > cap) {
     bool done = false;
     for (size_t x = 0; x < g.size() && !done; ++x)
@@ -260,11 +261,58 @@ void fuse(std::vector<Ix>& g, int cap, const char* spec) {
           done = true;
         }
       }
-    if (!done) fail(FCC_ERR_BAD_ARG, std::string("einsum group not reducible to 2 indices: ") + spec);
+    if (!done) return false;
   }
+  return true;
+}
+
+void fuse(std::vector<Ix>& g, int cap, const char* spec) {
+  if (!try_fuse(g, cap)) fail(FCC_ERR_BAD_ARG, std::string("einsum group not reducible to ") + std::to_string(cap) + " indices: " + spec);
+}
+
+int64_t gdim(const std::vector<Ix>& g) {
+  int64_t d = 1;
+  for (auto& x : g) d *= x.dim;
+  return d;
+}
+
+// pad a group to exactly 3 levels (slowest first)
+void pad3(std::vector<Ix>& g) { while (g.size() < 3) g.insert(g.begin(), Ix{1, {0, 0, 0}}); }
+
+// Tensor-core evaluation of C = alpha * A.B + beta * C (no batch index).
+void run_tc(TcEngine* tc, double alpha, const TView& A, const TView& B, double beta, const TView& C,
+            std::vector<Ix> gm, std::vector<Ix> gn, std::vector<Ix> gk, cudaStream_t s) {
+  // fastest-moving member last: the one with the smallest stride in the operand that is read along it
+  auto order = [](std::vector<Ix>& g, int op) {
+    std::stable_sort(g.begin(), g.end(), [op](const Ix& a, const Ix& b) { return std::llabs(a.s[op]) > std::llabs(b.s[op]); });
+  };
+  order(gm, 2);
+  order(gn, 2);
+  order(gk, 0);
+  pad3(gm); pad3(gn); pad3(gk);
+  const int64_t M = gdim(gm), N = gdim(gn), K = gdim(gk);
+  const int64_t Kp = packed_kp(K);
+  if ((int64_t)tc->bufA.n < M * Kp) tc->bufA.alloc(M * Kp);
+  if ((int64_t)tc->bufB.n < N * Kp) tc->bufB.alloc(N * Kp);
+  PackSpec pa{M, K, Kp, gm[1].dim, gm[2].dim, gm[0].s[0], gm[1].s[0], gm[2].s[0],
+              gk[1].dim, gk[2].dim, gk[0].s[0], gk[1].s[0], gk[2].s[0]};
+  PackSpec pb{N, K, Kp, gn[1].dim, gn[2].dim, gn[0].s[1], gn[1].s[1], gn[2].s[1],
+              gk[1].dim, gk[2].dim, gk[0].s[1], gk[1].s[1], gk[2].s[1]};
+  pack_split(A.p, pa, true, tc->bufA.p, s);
+  pack_split(B.p, pb, false, tc->bufB.p, s);
+  EpiMap ep{M, N, gm[1].dim, gm[2].dim, gm[0].s[2], gm[1].s[2], gm[2].s[2],
+            gn[1].dim, gn[2].dim, gn[0].s[2], gn[1].s[2], gn[2].s[2], alpha, beta, C.p, 0};
+  gemm_bf16x3(tc->bufA.p, M, 0, tc->bufB.p, N, 0, Kp, ep, tc->err, s);
+  tc->tc_calls++;
+  tc->tc_flops += 2.0 * (double)M * (double)N * (double)K;
 }
 
 }  // namespace
+
+TcEngine*& tc_engine() {
+  thread_local TcEngine* e = nullptr;
+  return e;
+}
 
 void einsum(double alpha, const char* spec, const TView& A, const TView& B, double beta, const TView& C,
             cudaStream_t s) {
@@ -293,10 +341,24 @@ void einsum(double alpha, const char* spec, const TView& A, const TView& B, doub
     else if (ia && ib) gk.push_back(ix);
     else fail(FCC_ERR_BAD_ARG, std::string("einsum index in one operand only: ") + spec);
   }
+  TcEngine* tc = tc_engine();
+  if (tc && tc->enabled && gb.empty()) {
+    const double flops = 2.0 * (double)gdim(gm) * (double)gdim(gn) * (double)gdim(gk);
+    std::vector<Ix> m3 = gm, n3 = gn, k3 = gk;
+    if (flops >= tc->min_flops && gdim(gm) >= tc->min_dim && gdim(gn) >= tc->min_dim && try_fuse(m3, 3) && try_fuse(n3, 3) &&
+        try_fuse(k3, 3)) {
+      run_tc(tc, alpha, A, B, beta, C, m3, n3, k3, s);
+      return;
+    }
+  }
   fuse(gb, 1, spec);
   fuse(gm, 2, spec);
   fuse(gn, 2, spec);
   fuse(gk, 2, spec);
+  if (tc) {
+    tc->f64_calls++;
+    tc->f64_flops += 2.0 * (double)gdim(gm) * (double)gdim(gn) * (double)gdim(gk) * (double)gdim(gb);
+  }
   // order pairs so the faster-moving member (second) has the smallest stride
   auto order = [](std::vector<Ix>& g, int op) {
     if (g.size() == 2 && std::llabs(g[0].s[op]) < std::llabs(g[1].s[op])) std::swap(g[0], g[1]);

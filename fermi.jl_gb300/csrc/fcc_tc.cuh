@@ -1,0 +1,59 @@
+// Split-BF16 tensor-core contraction: operand packing and the tcgen05 GEMM.
+#pragma once
+#include <cuda_bf16.h>
+
+#include "fcc_common.cuh"
+
+namespace fcc {
+
+// Gather spec of a packed operand: row r = (r1*rd2 + r2)*rd3 + r3 and column
+// k = (k1*kd2 + k2)*kd3 + k3 of a strided FP64 source; the destination is
+// R rows x Kp bf16 with the three split pieces at columns [0,K), [K,2K), [2K,3K).
+struct PackSpec {
+  int64_t R, K, Kp;
+  int64_t rd2, rd3, rs1, rs2, rs3;
+  int64_t kd2, kd3, ks1, ks2, ks3;
+};
+
+// Output scatter of the GEMM: element (m, n) goes to
+// C[m1*ms1 + m2*ms2 + m3*ms3 + n1*ns1 + n2*ns2 + n3*ns3] (FP64 or FP32) as
+// alpha * acc + beta * C.
+struct EpiMap {
+  int64_t M, N;
+  int64_t md2, md3, ms1, ms2, ms3;
+  int64_t nd2, nd3, ns1, ns2, ns3;
+  double alpha, beta;
+  void* C;
+  int c_fp32;
+};
+
+int64_t packed_kp(int64_t K);
+void pack_split(const double* src, const PackSpec& ps, bool is_a, __nv_bfloat16* dst, cudaStream_t s);
+// D = A' B'^T over Kp packed columns; rows a_row0.. of A' (a_rows total) and
+// b_row0.. of B' (b_rows total); err set to 1 if a bounded wait gave up.
+void gemm_bf16x3(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __nv_bfloat16* B, int64_t b_rows,
+                 int64_t b_row0, int64_t Kp, const EpiMap& ep, int* err, cudaStream_t s);
+
+// Engine state for einsum calls that run on the tensor cores: scratch for
+// the packed operands, the device error flag, the routing threshold and
+// counters of what ran.
+struct TcEngine {
+  bool enabled = false;
+  double min_flops = 5e7;
+  int64_t min_dim = 32;   // smallest M and N routed to the tensor cores
+  DBuf<__nv_bfloat16> bufA, bufB;
+  int* err = nullptr;
+  int64_t tc_calls = 0, f64_calls = 0;
+  double tc_flops = 0, f64_flops = 0;
+};
+
+// Current engine of this host thread (nullptr: every contraction is FP64).
+TcEngine*& tc_engine();
+
+struct TcScope {
+  TcEngine* prev;
+  explicit TcScope(TcEngine* e) : prev(tc_engine()) { tc_engine() = e; }
+  ~TcScope() { tc_engine() = prev; }
+};
+
+}  // namespace fcc

@@ -1,0 +1,69 @@
+// Test hooks (include/fermicc_testing.h): one contraction on the device.
+#include <cstring>
+
+#include "../../include/fermicc_testing.h"
+#include "fcc_tc.cuh"
+
+namespace {
+
+fcc::TView view_of(double* p, const int64_t* dims, int rank) {
+  fcc::TView t;
+  t.p = p;
+  t.rank = rank;
+  int64_t s = 1;
+  for (int k = rank - 1; k >= 0; --k) { t.dim[k] = dims[k]; t.str[k] = s; s *= dims[k]; }
+  return t;
+}
+
+int64_t count(const int64_t* dims, int rank) {
+  int64_t n = 1;
+  for (int k = 0; k < rank; ++k) n *= dims[k];
+  return n;
+}
+
+}  // namespace
+
+extern "C" int fcc_test_contract(int32_t precision, const char* spec, const double* A, const int64_t* adims,
+                                 int32_t arank, const double* B, const int64_t* bdims, int32_t brank, double* C,
+                                 const int64_t* cdims, int32_t crank, double alpha, double beta) {
+  try {
+    if (!spec || !A || !B || !C || !adims || !bdims || !cdims || arank < 1 || arank > 4 || brank < 1 || brank > 4 ||
+        crank < 1 || crank > 4)
+      return FCC_ERR_BAD_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return FCC_ERR_NO_DEVICE;
+    FCC_CUDA(cudaSetDevice(0));
+    cudaStream_t s;
+    FCC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    struct SDel { cudaStream_t s; ~SDel() { cudaStreamDestroy(s); } } sdel{s};
+    const int64_t na = count(adims, arank), nb = count(bdims, brank), nc = count(cdims, crank);
+    fcc::DBuf<double> dA, dB, dC;
+    dA.alloc(na); dB.alloc(nb); dC.alloc(nc);
+    fcc::DBuf<int> err;
+    err.alloc(1);
+    FCC_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+    FCC_CUDA(cudaMemcpyAsync(dA.p, A, na * 8, cudaMemcpyHostToDevice, s));
+    FCC_CUDA(cudaMemcpyAsync(dB.p, B, nb * 8, cudaMemcpyHostToDevice, s));
+    FCC_CUDA(cudaMemcpyAsync(dC.p, C, nc * 8, cudaMemcpyHostToDevice, s));
+    fcc::TcEngine eng;
+    eng.enabled = precision == FCC_PREC_MIXED;
+    eng.min_flops = 0.0;
+    eng.min_dim = 1;
+    eng.err = err.p;
+    {
+      fcc::TcScope scope(&eng);
+      fcc::einsum(alpha, spec, view_of(dA.p, adims, arank), view_of(dB.p, bdims, brank), beta,
+                  view_of(dC.p, cdims, crank), s);
+    }
+    if (precision == FCC_PREC_MIXED && eng.tc_calls != 1) return FCC_ERR_BAD_ARG;
+    int herr = 0;
+    FCC_CUDA(cudaMemcpyAsync(C, dC.p, nc * 8, cudaMemcpyDeviceToHost, s));
+    FCC_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FCC_CUDA(cudaStreamSynchronize(s));
+    return herr ? FCC_ERR_TIMEOUT : FCC_OK;
+  } catch (const fcc::Error& e) {
+    return e.code;
+  } catch (...) {
+    return FCC_ERR_CUDA;
+  }
+}

@@ -1,0 +1,339 @@
+// Split-BF16 tensor-core contraction for GB300 (sm_103a): tcgen05.mma with the
+// accumulator in TMEM, operands staged by TMA (cp.async.bulk.tensor) into
+// 128-byte-swizzled shared memory, an mbarrier pipeline between one producer
+// thread, one MMA-issuing thread and four epilogue warps.
+//
+// A FP64 contraction C = alpha * A.B + beta * C is evaluated as one BF16 GEMM
+// over a K-concatenated operand pair (three products, FP32 accumulation):
+//   A' = [hi(A) | hi(A) | lo(A)],  B' = [hi(B) | lo(B) | hi(B)]
+//   A'.B'^T = hi(A) hi(B) + hi(A) lo(B) + lo(A) hi(B)
+// with hi(x) = bf16(x) and lo(x) = bf16(x - hi(x)).  The pack kernel gathers
+// the operand from any strided tensor view (the index permutation of the
+// contraction is folded into it) and the epilogue scatters into any strided
+// output view, so no separate transpose pass exists.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+#include "fcc_tc.cuh"
+
+namespace fcc {
+
+namespace {
+
+constexpr int BM = 128;
+constexpr int BK = 64;                       // one 128-byte swizzle atom of bf16 per row
+constexpr int TC_THREADS = 192;              // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr uint64_t WAIT_NS = 2000000000ull;  // every mbarrier wait gives up after 2 s
+
+template <int BN>
+struct TcCfg {
+  static constexpr int STAGES = (BN == 256) ? 4 : 6;
+  static constexpr int A_BYTES = BM * BK * 2;
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int SMEM = STAGES * STAGE_BYTES + 1024;  // + alignment slack
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait on an mbarrier phase; false after WAIT_NS.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  uint64_t t0 = 0;
+  for (uint32_t it = 0;; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (it == 0) t0 = globaltimer();
+    else if ((it & 63) == 0 && globaltimer() - t0 > WAIT_NS) return false;
+  }
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* tm, int32_t x, int32_t y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle,
+// 8-row groups 1024 bytes apart (SBO), fixed version bits 46-48 = 0b001.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D F32, A and B BF16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+template <int BN>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    gemm_bf16_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t a_row0,
+                        int64_t b_row0, int num_k, EpiMap ep, int* err) {
+  using Cfg = TcCfg<BN>;
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[Cfg::STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[Cfg::STAGES];
+  __shared__ __align__(8) uint64_t acc_bar;
+  __shared__ uint32_t tmem_holder;
+  __shared__ int abort_flag;
+
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + Cfg::STAGES * Cfg::A_BYTES;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < Cfg::STAGES; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), 1);
+      mbar_init(smem_u32(&empty_bar[s]), 1);
+    }
+    mbar_init(smem_u32(&acc_bar), 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_holder)),
+                 "r"(BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_holder;
+  const int64_t m0 = (int64_t)blockIdx.x * BM;
+  const int64_t n0 = (int64_t)blockIdx.y * BN;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer
+    for (int kt = 0; kt < num_k; ++kt) {
+      const int s = kt % Cfg::STAGES;
+      const uint32_t ph = (kt / Cfg::STAGES) & 1;
+      if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1)) { atomicExch(&abort_flag, 1); break; }
+      if (*(volatile int*)&abort_flag) break;
+      const uint32_t fb = smem_u32(&full_bar[s]);
+      mbar_expect_tx(fb, Cfg::STAGE_BYTES);
+      tma_load_2d(smem_u32(sA + s * Cfg::A_BYTES), &tmA, kt * BK, (int32_t)(a_row0 + m0), fb);
+      tma_load_2d(smem_u32(sB + s * Cfg::B_BYTES), &tmB, kt * BK, (int32_t)(b_row0 + n0), fb);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer (single thread)
+    constexpr uint32_t idesc = idesc_bf16(BM, BN);
+    bool ok = true;
+    for (int kt = 0; kt < num_k; ++kt) {
+      const int s = kt % Cfg::STAGES;
+      const uint32_t ph = (kt / Cfg::STAGES) & 1;
+      if (!mbar_wait(smem_u32(&full_bar[s]), ph)) { atomicExch(&abort_flag, 1); ok = false; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint64_t ad = sw128_desc(smem_u32(sA + s * Cfg::A_BYTES));
+      const uint64_t bd = sw128_desc(smem_u32(sB + s * Cfg::B_BYTES));
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk) {
+        const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad + (uint64_t)(2 * kk)), "l"(bd + (uint64_t)(2 * kk)), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&empty_bar[s]))
+                   : "memory");
+    }
+    // signals the epilogue once every issued MMA has completed (also on abort)
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(&acc_bar))
+                 : "memory");
+    (void)ok;
+  } else if (warp >= 2) {
+    // ---------------- epilogue: TMEM -> registers -> strided global stores
+    bool ok = mbar_wait(smem_u32(&acc_bar), 0);
+    ok = __all_sync(0xffffffffu, ok);
+    if (!ok) atomicExch(&abort_flag, 1);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int q = warp & 3;              // TMEM lane quadrant this warp may access
+    const int row = q * 32 + lane;
+    const int64_t m = m0 + row;
+    const bool abort_now = __any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0);
+    if (ok && !abort_now) {
+      int64_t crow = 0;
+      if (m < ep.M) {
+        int64_t m3 = m % ep.md3, r = m / ep.md3;
+        int64_t m2 = r % ep.md2, m1 = r / ep.md2;
+        crow = m1 * ep.ms1 + m2 * ep.ms2 + m3 * ep.ms3;
+      }
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t r[32];
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (m < ep.M) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int64_t n = n0 + c0 + j;
+            if (n >= ep.N) break;
+            int64_t n3 = n % ep.nd3, rr = n / ep.nd3;
+            int64_t n2 = rr % ep.nd2, n1 = rr / ep.nd2;
+            const int64_t off = crow + n1 * ep.ns1 + n2 * ep.ns2 + n3 * ep.ns3;
+            const double val = ep.alpha * (double)__uint_as_float(r[j]);
+            if (ep.c_fp32) {
+              float* dst = static_cast<float*>(ep.C) + off;
+              *dst = (float)(ep.beta != 0.0 ? val + ep.beta * (double)*dst : val);
+            } else {
+              double* dst = static_cast<double*>(ep.C) + off;
+              *dst = ep.beta != 0.0 ? val + ep.beta * *dst : val;
+            }
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+  }
+  if (threadIdx.x == 0 && abort_flag) atomicExch(err, 1);
+}
+
+// ---------------------------------------------------------------- packing
+__device__ __forceinline__ void split2(double x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn((float)x);
+  lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
+}
+
+// dst[r][k'] (row pitch Kp) from src: piece p of k' = p*K + k holds hi or lo
+// of src(r, k) per `pattern` (bit p set = lo); columns >= 3K are zero.
+__global__ void pack_split_kernel(const double* __restrict__ src, PackSpec ps, int pattern,
+                                  __nv_bfloat16* __restrict__ dst) {
+  const int64_t total = ps.R * ps.Kp;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / ps.Kp, kk = t - r * ps.Kp;
+    __nv_bfloat16 outv = __float2bfloat16_rn(0.0f);
+    if (kk < 3 * ps.K) {
+      const int piece = (int)(kk / ps.K);
+      const int64_t k = kk - piece * ps.K;
+      int64_t r3 = r % ps.rd3, q = r / ps.rd3;
+      int64_t r2 = q % ps.rd2, r1 = q / ps.rd2;
+      int64_t k3 = k % ps.kd3, q2 = k / ps.kd3;
+      int64_t k2 = q2 % ps.kd2, k1 = q2 / ps.kd2;
+      const double x = src[r1 * ps.rs1 + r2 * ps.rs2 + r3 * ps.rs3 + k1 * ps.ks1 + k2 * ps.ks2 + k3 * ps.ks3];
+      __nv_bfloat16 hi, lo;
+      split2(x, hi, lo);
+      outv = ((pattern >> piece) & 1) ? lo : hi;
+    }
+    dst[t] = outv;
+  }
+}
+
+// -------------------------------------------------------- tensor maps
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+void get_encoder() {
+  std::call_once(g_encode_once, []() {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  });
+  if (!g_encode) fail(FCC_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+}
+
+CUtensorMap make_map(const __nv_bfloat16* base, int64_t rows, int64_t Kp, int box_rows) {
+  get_encoder();
+  if (Kp % BK != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0)
+    fail(FCC_ERR_BAD_ARG, "packed operand misaligned for TMA");
+  CUtensorMap tm;
+  std::memset(&tm, 0, sizeof(tm));
+  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(&tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(base), dims, strides, box,
+                        estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) fail(FCC_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  return tm;
+}
+
+template <int BN>
+void launch_tc(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __nv_bfloat16* B, int64_t b_rows,
+               int64_t b_row0, int64_t Kp, const EpiMap& ep, int* err, cudaStream_t s) {
+  using Cfg = TcCfg<BN>;
+  static std::once_flag attr_once;
+  std::call_once(attr_once, []() {
+    cudaFuncSetAttribute(gemm_bf16_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM);
+  });
+  CUtensorMap ta = make_map(A, a_rows, Kp, BM);
+  CUtensorMap tb = make_map(B, b_rows, Kp, BN);
+  dim3 grid((unsigned)((ep.M + BM - 1) / BM), (unsigned)((ep.N + BN - 1) / BN));
+  if (grid.y > 65535) fail(FCC_ERR_BAD_ARG, "tensor-core grid too large");
+  gemm_bf16_tc_kernel<BN><<<grid, TC_THREADS, Cfg::SMEM, s>>>(ta, tb, a_row0, b_row0, (int)(Kp / BK), ep, err);
+  FCC_CHECK_LAUNCH();
+}
+
+}  // namespace
+
+int64_t packed_kp(int64_t K) { return ((3 * K + BK - 1) / BK) * BK; }
+
+void pack_split(const double* src, const PackSpec& ps, bool is_a, __nv_bfloat16* dst, cudaStream_t s) {
+  const int64_t total = ps.R * ps.Kp;
+  if (total <= 0) return;
+  const int threads = 256;
+  const int64_t blocks = std::min<int64_t>((total + threads - 1) / threads, 152 * 64);
+  // A' = [hi | hi | lo] (lo in piece 2), B' = [hi | lo | hi] (lo in piece 1)
+  pack_split_kernel<<<(unsigned)blocks, threads, 0, s>>>(src, ps, is_a ? 0b100 : 0b010, dst);
+  FCC_CHECK_LAUNCH();
+}
+
+void gemm_bf16x3(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __nv_bfloat16* B, int64_t b_rows,
+                 int64_t b_row0, int64_t Kp, const EpiMap& ep, int* err, cudaStream_t s) {
+  if (ep.M <= 0 || ep.N <= 0) return;
+  if (Kp <= 0 || Kp % BK) fail(FCC_ERR_BAD_ARG, "bad packed K");
+  if (ep.N >= 256) launch_tc<256>(A, a_rows, a_row0, B, b_rows, b_row0, Kp, ep, err, s);
+  else launch_tc<128>(A, a_rows, a_row0, B, b_rows, b_row0, Kp, ep, err, s);
+}
+
+}  // namespace fcc

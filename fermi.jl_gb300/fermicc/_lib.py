@@ -24,9 +24,10 @@ FCC_ERR_NO_DEVICE = -8
 FCC_PREC_FP64 = 0
 FCC_PREC_MIXED = 1
 
-# every symbol the header declares
+# every symbol include/fermicc.h declares, and the test hooks of include/fermicc_testing.h
 EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess",
            "fcc_ccsd_run", "fcc_get_amps", "fcc_triples", "fcc_destroy", "fcc_strerror", "fcc_last_error")
+TEST_EXPORTS = ("fcc_test_contract",)
 
 
 class FccOpts(ctypes.Structure):
@@ -79,6 +80,10 @@ def load():
     lib.fcc_strerror.restype = ctypes.c_char_p
     lib.fcc_last_error.argtypes = [vp]
     lib.fcc_last_error.restype = ctypes.c_char_p
+    i64p = ctypes.POINTER(ctypes.c_int64)
+    lib.fcc_test_contract.argtypes = [i32, ctypes.c_char_p, dp, i64p, i32, dp, i64p, i32, dp, i64p, i32,
+                                      ctypes.c_double, ctypes.c_double]
+    lib.fcc_test_contract.restype = ctypes.c_int
     for name in ("fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess", "fcc_ccsd_run",
                  "fcc_get_amps", "fcc_triples"):
         getattr(lib, name).restype = ctypes.c_int

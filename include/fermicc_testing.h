@@ -1,0 +1,28 @@
+/*
+ * fermicc_testing.h -- test hooks of libfermicc.so.
+ *
+ * These entry points have no counterpart in Fermi.jl.  They expose single
+ * device contractions so the test suite can check each kernel against a
+ * host reference in isolation.
+ */
+#ifndef FERMICC_TESTING_H
+#define FERMICC_TESTING_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* C = alpha * einsum(spec, A, B) + beta * C on device 0 for row-major host
+ * tensors (rank <= 4 each).  precision FCC_PREC_FP64 runs the DMMA kernel;
+ * FCC_PREC_MIXED forces the split-BF16 tensor-core kernel (error if the
+ * contraction cannot be expressed for it).  Returns an fcc status code. */
+int fcc_test_contract(int32_t precision, const char* spec, const double* A, const int64_t* adims, int32_t arank,
+                      const double* B, const int64_t* bdims, int32_t brank, double* C, const int64_t* cdims,
+                      int32_t crank, double alpha, double beta);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FERMICC_TESTING_H */

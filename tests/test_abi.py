@@ -17,13 +17,13 @@ def lib():
     return _lib.load()
 
 
-def declared_functions():
-    text = open(os.path.join(ROOT, "include", "fermicc.h")).read()
+def declared_functions(header="fermicc.h"):
+    text = open(os.path.join(ROOT, "include", header)).read()
     return sorted(set(re.findall(r"\b(fcc_[a-z_0-9]+)\s*\(", text)))
 
 
 def test_every_declared_symbol_is_exported(lib):
-    names = declared_functions()
+    names = declared_functions() + declared_functions("fermicc_testing.h")
     assert "fcc_ccsd_run" in names and "fcc_triples" in names
     for n in names:
         assert hasattr(lib, n), n
@@ -32,6 +32,7 @@ def test_every_declared_symbol_is_exported(lib):
 def test_python_binding_covers_header():
     from fermicc import _lib
     assert sorted(_lib.EXPORTS) == declared_functions()
+    assert sorted(_lib.TEST_EXPORTS) == declared_functions("fermicc_testing.h")
 
 
 def test_default_options_are_fermis(lib):

@@ -1,0 +1,59 @@
+"""Single-contraction checks of the two device kernels against numpy.
+
+FP64 (DMMA) must agree to round-off; the split-BF16 tensor-core kernel
+(three products, FP32 accumulation) to about 1e-5 of the largest |C|.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    ("mk,nk->mn", (128, 64), (128, 64), (128, 128)),
+    ("mk,nk->mn", (200, 70), (130, 70), (200, 130)),
+    ("ik,kj->ij", (333, 250), (250, 97), (333, 97)),
+    ("ijcd,acbd->ijab", (6, 5, 9, 11), (7, 9, 8, 11), (6, 5, 7, 8)),
+    ("kjbc,kiac->ijab", (5, 6, 7, 8), (5, 4, 9, 8), (4, 6, 9, 7)),
+    ("lb,lca->abc", (9, 40), (9, 33, 37), (37, 40, 33)),
+    ("Qai,Qbj->ijab", (50, 20, 6), (50, 21, 7), (6, 7, 20, 21)),
+    ("abd,cd->abc", (17, 19, 150), (300, 150), (17, 19, 300)),
+]
+
+
+def _run(prec, spec, A, B, C, alpha=1.0, beta=0.0):
+    from fermicc import _lib
+    lib = _lib.load()
+    i64 = lambda shape: (ctypes.c_int64 * len(shape))(*shape)
+    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    A = np.ascontiguousarray(A); B = np.ascontiguousarray(B)
+    out = np.ascontiguousarray(C.copy())
+    rc = lib.fcc_test_contract(prec, spec.encode(), dp(A), i64(A.shape), A.ndim, dp(B), i64(B.shape), B.ndim,
+                               dp(out), i64(out.shape), out.ndim, alpha, beta)
+    return rc, out
+
+
+@pytest.mark.parametrize("spec,sa,sb,sc", CASES)
+def test_fp64_contraction(spec, sa, sb, sc):
+    rng = np.random.default_rng(0)
+    A, B, C = rng.standard_normal(sa), rng.standard_normal(sb), rng.standard_normal(sc)
+    rc, out = _run(0, spec, A, B, C, 0.7, -1.3)
+    assert rc == 0
+    ref = 0.7 * np.einsum(spec, A, B) - 1.3 * C
+    assert np.abs(out - ref).max() < 1e-12 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("spec,sa,sb,sc", CASES)
+def test_split_bf16_tensor_core_contraction(spec, sa, sb, sc):
+    rng = np.random.default_rng(1)
+    A, B, C = rng.standard_normal(sa), rng.standard_normal(sb), rng.standard_normal(sc)
+    rc, out = _run(1, spec, A, B, C, 1.0, 0.0)
+    assert rc == 0
+    ref = np.einsum(spec, A, B)
+    err = np.abs(out - ref).max() / np.abs(ref).max()
+    assert err < 3e-5, err
+    rc, out2 = _run(1, spec, A, B, C, -0.5, 2.0)
+    assert rc == 0
+    ref2 = -0.5 * ref + 2.0 * C
+    assert np.abs(out2 - ref2).max() / np.abs(ref2).max() < 3e-5
