@@ -1,0 +1,297 @@
+#!/usr/bin/env python
+"""DF-CCSD(T) time-to-solution on a seeded (H2O)8 cluster, one GB300.
+
+Workload: (H2O)8 on a 2x2x2 lattice (seed 0), stand-in cc-pVDZ / cc-pVDZ-RI
+shell structure: 192 basis functions, 32 active occupied (8 frozen core), 152
+virtual, 672 fitting functions.  One "step" is one full solve: CCSD from the
+MP2 guess to convergence (residual rms < 1e-8 and |dE| < 1e-8 Eh) followed
+by (T).  The form measured is the mixed one (split-BF16 tensor-core
+contractions, FP64 finish and FP64 energies); ``--form fp64`` measures the
+plain FP64 form.
+
+JSON line (rank 0): ``value`` = device time-to-solution in seconds with the
+integrals resident in HBM (CUDA events on the library's stream); ``e2e`` =
+the same solve through the C ABI from host buffers (context creation,
+host->device upload of the three-index factors, solve, device->host read of
+T1/T2), host wall clock; ``roofline`` for the dominant kernel; ``cpu_baseline``
+= the CPU restatement of Fermi's algorithm (the oracle) timed on a bounded
+sample of the same workload on this host and scaled to a full solve.
+
+``--impl reference`` times that CPU restatement alone (Fermi.jl itself cannot
+run here: no Julia, no libcint, no basis files) and prints its line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "fermi.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "DF-CCSD(T) time-to-solution (H2O)8/cc-pVDZ: mixed+learned vs FP64 GPU @1µEh"
+E_CONV = 1e-8
+MAX_RMS = 1e-8
+# FP64-form iteration count of this workload at these criteria (the CPU
+# restatement follows the same iteration sequence); used to scale the
+# one-iteration CPU sample to a full solve.
+FP64_ITERATIONS = 19
+FP64_PEAK_TFLOPS = 1.05     # measured DMMA / DFMA peak of this GB300 pool (own probe)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--waters", type=int, default=8)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def algorithmic_flops(o, v, Q):
+    """Leading-order flops of one CCSD iteration and of (T)."""
+    f_it = 2 * o**2 * v**4 + 2 * Q * v**4 + 12 * o**3 * v**3
+    f_t = 2 * o * (o + 1) * (o + 2) * v**3 * (v + o)
+    return f_it, f_t
+
+
+class Clocks:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.samples, self.index, self.proc = [], index, None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = sorted(float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit())
+        mx = max(float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 5 + k and s[5 + k] == "Active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def cpu_sample(inp, ntrip=8):
+    """The CPU restatement of Fermi's algorithm on a bounded sample of the
+    workload: one full CCSD iteration (RCCSDHelper.jl update_amp at the MP2
+    guess) and `ntrip` (T) triplets spread over the i >= j >= k list."""
+    import numpy as np
+    from oracle import rccsd as R
+    from oracle import triples as T
+    I = R.df_blocks(inp.Boo, inp.Bov, inp.Bvv)
+    D1, D2 = R.denominators(inp.eps_o, inp.eps_v)
+    T1, T2 = R.mp2_guess(I, D1, D2)
+    t0 = time.perf_counter()
+    R.update_amp(T1, T2, I, D1, D2, lambda a, b: R.ladder_df(a, b, inp.Bvv))
+    t_it = time.perf_counter() - t0
+    trip = T.triplet_list(inp.o)
+    pick = trip[:: max(1, len(trip) // ntrip)][:ntrip]
+    t0 = time.perf_counter()
+    T.triples_ijk(T1, T2, I["OVVV"], I["OOOV"], I["OVOV"], inp.eps_o, inp.eps_v, triplets=pick)
+    t_t = (time.perf_counter() - t0) / len(pick) * len(trip)
+    value = FP64_ITERATIONS * t_it + t_t
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    return {"value": value, "unit": "s", "cores": cores, "kind": "port",
+            "sample": (f"1 CCSD iteration ({t_it:.1f} s, scaled x{FP64_ITERATIONS}) + {len(pick)} of {len(trip)} "
+                       f"(T) triplets ({t_t:.1f} s scaled); numpy/BLAS restatement of RCCSDHelper.jl + ijk.jl")}
+
+
+def run_reference(args, inp):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    vals = []
+    for it in range(args.warmup + args.steps):
+        cb = cpu_sample(inp)
+        if it >= args.warmup:
+            vals.append(cb["value"])
+    value = sum(vals) / len(vals)
+    cb["value"] = value
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded water cluster)",
+           "config": {"workload": f"(H2O){args.waters} seed {args.seed} DF-RCCSD(T)", "o": inp.o, "v": inp.v,
+                      "naux": inp.naux, "e_conv": E_CONV, "max_rms": MAX_RMS},
+           "cpu_baseline": cb, "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    from fermicc.inputs import scf
+    inp = scf.water_inputs(args.waters, seed=args.seed)
+    if args.impl == "reference":
+        run_reference(args, inp)
+        return
+    import numpy as np
+    import torch
+    from fermicc import Options, RCCSD, RCCSDpT, _lib
+    from fermicc.rccsd import Context
+
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    lib = _lib.load()
+    Options.reset()
+    Options.set("cc_gpu_device", local)
+    Options.set("cc_gpu_precision", args.form)
+    Options.set("pt_gpu_precision", args.form)
+    Options.set("cc_e_conv", E_CONV)
+    Options.set("cc_max_rms", MAX_RMS)
+    Options.set("cc_max_iter", 100)
+
+    ctx = Context(inp, device=local)
+    stream = torch.cuda.ExternalStream(lib.fcc_stream(ctx.h))
+
+    def solve():
+        ctx.lib.fcc_set_guess(ctx.h, None, None)
+        ccsd = RCCSD.compute(inp, context=ctx)
+        pt = RCCSDpT.compute(ccsd, inp)
+        return ccsd, pt
+
+    for _ in range(args.warmup):
+        solve()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = lib.fcc_stat_launches()
+    times, results = [], []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ccsd, pt = solve()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            results.append((ccsd, pt))
+    torch.cuda.synchronize()
+    launches = lib.fcc_stat_launches() - launches0
+    t_step = sum(times) / len(times)
+    if world > 1:
+        tt = torch.tensor([t_step], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(tt.item())
+    ccsd, pt = results[-1]
+    it_kinds = [l["precision"] for l in ccsd.iterations]
+    f_it, f_t = algorithmic_flops(inp.o, inp.v, inp.naux)
+    # dominant kernel by time: the FP64 DMMA contraction kernel of the FP64
+    # residual evaluations (the split-BF16 iterations and (T) are far shorter)
+    f64_iters = [l for l in ccsd.iterations if l["precision"] == 0]
+    t64 = sum(l["seconds"] for l in f64_iters) / max(1, len(f64_iters))
+    achieved = f_it / t64 / 1e12 if f64_iters else None
+    roof = {"bound": "tensor", "kernel": "contract_f64_kernel (DMMA m8n8k4) within one FP64 residual evaluation",
+            "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+            "frac": (achieved / FP64_PEAK_TFLOPS) if achieved else None, "traffic": None,
+            "peak_source": "own measurement (DMMA probe); MEASURED_PEAKS.json has no FP64 figure"}
+
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        hB = [np.asfortranarray(x) for x in (inp.Boo, inp.Bov, inp.Bvv)]
+        pinned = []
+        for x in hB:
+            t = torch.empty(x.size, dtype=torch.float64, pin_memory=True).numpy()
+            t[:] = x.ravel(order="F")
+            pinned.append(t)
+        h2d = sum(x.nbytes for x in pinned) + 8 * (inp.o + inp.v)
+        d2h = 8 * (inp.o * inp.v + inp.o**2 * inp.v**2)
+        t0 = time.perf_counter()
+        h = ctypes.c_void_p()
+        assert lib.fcc_create(ctypes.byref(h), inp.o, inp.v, inp.naux, local) == 0
+        dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        eo = np.ascontiguousarray(inp.eps_o)
+        ev = np.ascontiguousarray(inp.eps_v)
+        assert lib.fcc_upload_df(h, dp(pinned[0]), dp(pinned[1]), dp(pinned[2]), dp(eo), dp(ev), inp.e_ref) == 0
+        opts = _lib.FccOpts()
+        lib.fcc_default_opts(ctypes.byref(opts))
+        opts.precision = 1 if args.form == "mixed" else 0
+        opts.e_conv, opts.max_rms, opts.max_iter = E_CONV, MAX_RMS, 100
+        res = _lib.FccCCSDResult()
+        rc = lib.fcc_ccsd_run(h, ctypes.byref(opts), None, 0, ctypes.byref(res))
+        assert rc == 0, rc
+        et = ctypes.c_double()
+        assert lib.fcc_triples(h, opts.precision, ctypes.byref(et)) == 0
+        T1 = torch.empty(inp.o * inp.v, dtype=torch.float64, pin_memory=True).numpy()
+        T2 = torch.empty(inp.o**2 * inp.v**2, dtype=torch.float64, pin_memory=True).numpy()
+        assert lib.fcc_get_amps(h, dp(T1), dp(T2)) == 0
+        lib.fcc_destroy(h)
+        t_e2e = time.perf_counter() - t0
+        e2e = {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "energy": res.energy + et.value}
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        cpu = cpu_sample(inp)
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": t_step, "unit": "s", "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
+               "vs_baseline": None, "dtype": "bf16x3+f64" if args.form == "mixed" else "f64",
+               "data": "synthetic (seeded water cluster, stand-in basis)",
+               "config": {"workload": f"(H2O){args.waters} seed {args.seed} DF-RCCSD(T)", "form": args.form,
+                          "o": inp.o, "v": inp.v, "naux": inp.naux, "e_conv": E_CONV, "max_rms": MAX_RMS,
+                          "parallelism": "replicas" if world > 1 else "single GPU",
+                          "l2": "working set > L2 (T2 189 MB, factors 160 MB)"},
+               "e_ccsd": ccsd.energy, "e_t": pt.correction, "e_total": pt.energy,
+               "iterations": len(ccsd.iterations), "iteration_kinds": it_kinds,
+               "fp64_iteration_s": t64 if f64_iters else None,
+               "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+               "clocks": clk.summary()}
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -362,7 +362,7 @@ double cc_energy(fcc_ctx* c, const double* t1, const double* t2) {
 // Full CCSD residuals r1 = Omega_ia, r2 = Omega_ijab (zero at convergence) for
 // the current t1, t2; the reference's pre-denominator amplitudes are
 // r + D * t (RCCSDHelper.jl:304-349).
-void residual_fp64(fcc_ctx* c) {
+void residual(fcc_ctx* c) {
   cudaStream_t s = c->stream;
   const int64_t o = c->o, v = c->v, Q = c->Q, n = c->n;
   TView t1 = rm(c->t1.p, {o, v});
@@ -491,8 +491,16 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
   fcc_opts op = *opt;
   if (op.max_iter < 0 || op.ndiis < 1 || op.ndiis > MAX_DIIS || op.diis_relax < 1 || op.damp < 0 || op.damp >= 1)
     fail(FCC_ERR_BAD_ARG, "invalid CC options");
-  if (op.precision != FCC_PREC_FP64)
-    fail(FCC_ERR_BAD_ARG, "this build runs FCC_PREC_FP64 only");
+  if (op.precision != FCC_PREC_FP64 && op.precision != FCC_PREC_MIXED)
+    fail(FCC_ERR_BAD_ARG, "precision must be FCC_PREC_FP64 or FCC_PREC_MIXED");
+  if (op.precision == FCC_PREC_MIXED && !(op.mixed_switch_rms > 0))
+    fail(FCC_ERR_BAD_ARG, "mixed_switch_rms must be positive");
+  int phase = op.precision;  // mixed: split-BF16 contractions until the switch, then FP64
+  if (!c->dev_err.p) c->dev_err.alloc(1);
+  FCC_CUDA(cudaMemsetAsync(c->dev_err.p, 0, sizeof(int), s));
+  c->tc.err = c->dev_err.p;
+  double best_rms = 1e300;
+  int stalled = 0;
   bool diis = op.diis != 0;
   bool fp32err = op.diis_prec != 64;
 
@@ -634,20 +642,60 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
   };
 
   int status = FCC_OK;
-  while (std::fabs(dE) > op.e_conv || rms > op.max_rms) {                   // RCCSDa.jl:178
+  bool conv_final = false;
+  // Iteration kinds: FP64 residual; split-BF16 residual (mixed form, first
+  // phase); split-BF16 residual plus the FP64 defect delta = R64(T0) - Rmix(T0)
+  // of the last FP64 evaluation (mixed form, finish).  The mixed form ends
+  // only on an FP64 residual evaluation that meets the criteria, so its
+  // converged amplitudes are the FP64 fixed point.
+  enum { K_F64 = 0, K_MIX = 1, K_CORR = 2 };
+  int kind = (phase == FCC_PREC_MIXED) ? K_MIX : K_F64;
+  bool finish = false;           // mixed form: in the defect-corrected finish
+  int inner = 0;
+  double inner_tol = 0.0;
+  DBuf<double> del1, del2;
+  auto reset_diis = [&]() { for (auto* d : {&D1s, &D2s}) std::fill(d->valid.begin(), d->valid.end(), 0); };
+  while (true) {
     if (ite > op.max_iter) { status = FCC_NO_CONVERGE; break; }            // :179-182
     FCC_CUDA(cudaEventRecord(ev0, s));
     // T1 .= newT1; T2 .= newT2                                              // :185-186
     if (cur1 != c->t1.p) FCC_CUDA(cudaMemcpyAsync(c->t1.p, cur1, sizeof(double) * len1, cudaMemcpyDeviceToDevice, s));
     if (cur2 != c->t2.p) FCC_CUDA(cudaMemcpyAsync(c->t2.p, cur2, sizeof(double) * len2, cudaMemcpyDeviceToDevice, s));
     double oldE = Ecc;
-    residual_fp64(c);                                                      // :190
+    const int iter_kind = kind;
+    if (kind == K_F64 && finish) {
+      // FP64 evaluation inside the mixed finish: R64 and delta = R64 - Rmix
+      if (!del1.p) { del1.alloc(len1); del2.alloc(len2); }
+      reset_diis();
+      { TcScope scope(nullptr); residual(c); }
+      FCC_CUDA(cudaMemcpyAsync(del1.p, c->r1.p, sizeof(double) * len1, cudaMemcpyDeviceToDevice, s));
+      FCC_CUDA(cudaMemcpyAsync(del2.p, c->r2.p, sizeof(double) * len2, cudaMemcpyDeviceToDevice, s));
+      { TcScope scope(&c->tc); c->tc.enabled = true; residual(c); }
+      axpby_flat_kernel<<<grid_for(len1), 256, 0, s>>>(del1.p, c->r1.p, len1, 1.0, -1.0);
+      FCC_CHECK_LAUNCH();
+      axpby_flat_kernel<<<grid_for(len2), 256, 0, s>>>(del2.p, c->r2.p, len2, 1.0, -1.0);
+      FCC_CHECK_LAUNCH();
+      axpby_flat_kernel<<<grid_for(len1), 256, 0, s>>>(c->r1.p, del1.p, len1, 1.0, 1.0);
+      FCC_CHECK_LAUNCH();
+      axpby_flat_kernel<<<grid_for(len2), 256, 0, s>>>(c->r2.p, del2.p, len2, 1.0, 1.0);
+      FCC_CHECK_LAUNCH();
+    } else {
+      TcScope scope(kind == K_F64 ? nullptr : &c->tc);
+      c->tc.enabled = kind != K_F64;
+      residual(c);                                                         // :190
+      if (kind == K_CORR) {
+        axpby_flat_kernel<<<grid_for(len1), 256, 0, s>>>(c->r1.p, del1.p, len1, 1.0, 1.0);
+        FCC_CHECK_LAUNCH();
+        axpby_flat_kernel<<<grid_for(len2), 256, 0, s>>>(c->r2.p, del2.p, len2, 1.0, 1.0);
+        FCC_CHECK_LAUNCH();
+      }
+    }
     double ss1, ss2, e_dummy, e_new;
     run_update(2, D1s, c->dvec1, c->derr1s, c->derr1d, c->t1.p, c->r1.p, tn1, &cur1, nullptr, &ss1, &e_dummy);
     run_update(4, D2s, c->dvec2, c->derr2s, c->derr2d, c->t2.p, c->r2.p, tn2, &cur2, cur1, &ss2, &e_new);
     double r1 = std::sqrt(ss1 / (double)len1), r2 = std::sqrt(ss2 / (double)len2);   // :193-194
     bool did = false;
-    if (diis && ite >= op.diis_start && ite % op.diis_relax == 0) {        // :204
+    if (diis && ite >= op.diis_start && ite % op.diis_relax == 0 && D1s.count() >= 2 && D2s.count() >= 2) {   // :204
       double e1d;
       extrapolate(2, D1s, c->dvec1, c->derr1s, c->derr1d, tx1, nullptr, &e1d);
       extrapolate(4, D2s, c->dvec2, c->derr2s, c->derr2d, tx2, tx1.p, &e_new);
@@ -671,19 +719,42 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
     Ecc = e_new;                                                           // :218
     rms = std::max(r1, r2);                                                // :220
     dE = Ecc - oldE;                                                       // :221
+    bool converged = iter_kind == K_F64 && std::fabs(dE) < op.e_conv && rms < op.max_rms;   // :178
+    if (phase == FCC_PREC_MIXED && !converged) {
+      if (iter_kind == K_MIX) {
+        // leave the split-BF16 phase once the residual is below the threshold,
+        // or when it stops improving (its noise floor)
+        if (rms < best_rms * 0.7) { best_rms = std::min(best_rms, rms); stalled = 0; }
+        else ++stalled;
+        if (rms < op.mixed_switch_rms || stalled >= 3) { finish = true; kind = K_F64; }
+      } else if (iter_kind == K_F64) {
+        kind = K_CORR;
+        inner = 0;
+        inner_tol = std::max(1e-3 * rms, 0.1 * op.max_rms);
+      } else {
+        ++inner;
+        if (rms < inner_tol || inner >= 12) kind = K_F64;
+      }
+    }
     FCC_CUDA(cudaEventRecord(ev1, s));
     FCC_CUDA(cudaEventSynchronize(ev1));
     float ms = 0;
     FCC_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
     if (!std::isfinite(Ecc) || !std::isfinite(rms)) { status = FCC_ERR_NAN; }
+    if (iter_kind != K_F64 || finish) {
+      int herr = 0;
+      FCC_CUDA(cudaMemcpy(&herr, c->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+      if (herr) { status = FCC_ERR_TIMEOUT; }
+    }
     if (log && nlog < log_cap) {
       fcc_iter_stats& L = log[nlog];
-      L.ite = ite; L.diis = did; L.precision = FCC_PREC_FP64; L.pad = 0;
+      L.ite = ite; L.diis = did; L.precision = iter_kind; L.pad = 0;
       L.energy = Ecc; L.dE = dE; L.rms = rms; L.seconds = ms * 1e-3;
     }
     ++nlog;
     ++ite;
-    if (status == FCC_ERR_NAN) break;
+    if (status == FCC_ERR_NAN || status == FCC_ERR_TIMEOUT) break;
+    if (converged) { conv_final = true; break; }
   }
   // keep the final amplitudes in c->t1 / c->t2
   if (cur1 != c->t1.p) FCC_CUDA(cudaMemcpyAsync(c->t1.p, cur1, sizeof(double) * len1, cudaMemcpyDeviceToDevice, s));
@@ -698,7 +769,7 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
     res->e_conv = dE;
     res->t_conv = rms;
     res->iterations = nlog;
-    res->converged = (std::fabs(dE) < op.e_conv && rms < op.max_rms) ? 1 : 0;   // :231
+    res->converged = conv_final ? 1 : 0;                                   // :231
   }
   c->have_ccsd = true;
   return status;

@@ -8,6 +8,7 @@
 // (about 1 TFLOP/s per GPU) is the bound of this kernel; a 64x64 tile with
 // 16-deep K steps staged through shared memory keeps it saturated.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <map>
 
@@ -167,6 +168,34 @@ __global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restri
   }
 }
 
+// N == 1 (matrix-vector): one warp per output row, lanes stride over K.
+__global__ void gemv_f64_kernel(const double* __restrict__ A, const double* __restrict__ B, double* __restrict__ C,
+                                CtrDesc d) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t bz = blockIdx.y;
+  A += bz * d.a_b;
+  B += bz * d.b_b;
+  C += bz * d.c_b;
+  for (int64_t m = warp; m < d.M; m += nwarps) {
+    const int64_t m1 = m / d.M2, m2 = m - m1 * d.M2;
+    const double* a = A + m1 * d.a_m1 + m2 * d.a_m2;
+    double s = 0.0;
+    for (int64_t k = lane; k < d.K; k += 32) {
+      const int64_t k1 = k / d.K2, k2 = k - k1 * d.K2;
+      s += a[k1 * d.a_k1 + k2 * d.a_k2] * B[k1 * d.b_k1 + k2 * d.b_k2];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      double* dst = C + m1 * d.c_m1 + m2 * d.c_m2;
+      double v = d.alpha * s;
+      if (d.beta != 0.0) v += d.beta * *dst;
+      *dst = v;
+    }
+  }
+}
+
 __global__ void axpby4_kernel(const double* __restrict__ in, double* __restrict__ out, int64_t d0,
                               int64_t d1, int64_t d2, int64_t d3, int64_t si0, int64_t si1, int64_t si2,
                               int64_t si3, int64_t so0, int64_t so1, int64_t so2, int64_t so3,
@@ -192,6 +221,12 @@ void contract_f64_launch(const double* A, const double* B, double* C, const CtrD
   int64_t gm = (d.M + BM - 1) / BM, gn = (d.N + BN - 1) / BN;
   if (gn > 65535 || d.batch > 65535) fail(FCC_ERR_BAD_ARG, "contraction grid too large");
   if (d.K <= 0) fail(FCC_ERR_BAD_ARG, "empty contraction index");
+  if (d.N == 1) {
+    const int64_t blocks = std::min<int64_t>((d.M + 7) / 8, 152 * 16);
+    gemv_f64_kernel<<<dim3((unsigned)blocks, (unsigned)d.batch), 256, 0, s>>>(A, B, C, d);
+    FCC_CHECK_LAUNCH();
+    return;
+  }
   dim3 grid((unsigned)gm, (unsigned)gn, (unsigned)d.batch);
   contract_f64_kernel<<<grid, NT, 0, s>>>(A, B, C, d, d.a_m2 == 1 ? 1 : 0, d.b_n2 == 1 ? 1 : 0);
   FCC_CHECK_LAUNCH();
@@ -300,14 +335,21 @@ void run_tc(TcEngine* tc, double alpha, const TView& A, const TView& B, double b
               gk[1].dim, gk[2].dim, gk[0].s[1], gk[1].s[1], gk[2].s[1]};
   pack_split(A.p, pa, true, tc->bufA.p, s);
   pack_split(B.p, pb, false, tc->bufB.p, s);
-  EpiMap ep{M, N, gm[1].dim, gm[2].dim, gm[0].s[2], gm[1].s[2], gm[2].s[2],
-            gn[1].dim, gn[2].dim, gn[0].s[2], gn[1].s[2], gn[2].s[2], alpha, beta, C.p, 0};
+  EpiMap ep;
+  ep.M = M; ep.N = N;
+  ep.md2 = gm[1].dim; ep.md3 = gm[2].dim; ep.ms1 = gm[0].s[2]; ep.ms2 = gm[1].s[2]; ep.ms3 = gm[2].s[2];
+  ep.nd2 = gn[1].dim; ep.nd3 = gn[2].dim; ep.ns1 = gn[0].s[2]; ep.ns2 = gn[1].s[2]; ep.ns3 = gn[2].s[2];
+  ep.alpha = alpha; ep.beta = beta; ep.C = C.p; ep.mode = EPI_F64;
   gemm_bf16x3(tc->bufA.p, M, 0, tc->bufB.p, N, 0, Kp, ep, tc->err, s);
   tc->tc_calls++;
   tc->tc_flops += 2.0 * (double)M * (double)N * (double)K;
 }
 
 }  // namespace
+
+static std::atomic<int64_t> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 TcEngine*& tc_engine() {
   thread_local TcEngine* e = nullptr;

@@ -245,7 +245,14 @@ int fcc_set_guess(fcc_ctx* c, const double* T1, const double* T2) {
   if (!c) return FCC_ERR_BAD_ARG;
   return guarded(c, [&]() {
     if (!c->have_ints) fcc::fail(FCC_ERR_STATE, "upload integrals first");
-    if (!T1 || !T2) fcc::fail(FCC_ERR_BAD_ARG, "null amplitudes");
+    if (!T1 && !T2) {  // back to the MP2 guess, built on the device
+      fcc::make_mp2_guess(c);
+      FCC_CUDA(cudaStreamSynchronize(c->stream));
+      c->have_guess = false;
+      c->have_ccsd = false;
+      return FCC_OK;
+    }
+    if (!T1 || !T2) fcc::fail(FCC_ERR_BAD_ARG, "give both amplitudes or neither");
     const int64_t o = c->o, v = c->v;
     if (!finite_all(T1, o * v) || !finite_all(T2, o * o * v * v)) fcc::fail(FCC_ERR_NAN, "non-finite guess amplitudes");
     upload_view(c, T1, o * v, cm(nullptr, {o, v}), rm(c->t1.p, {o, v}));
@@ -283,8 +290,8 @@ int fcc_triples(fcc_ctx* c, int32_t precision, double* et_out) {
   return guarded(c, [&]() {
     if (!et_out) fcc::fail(FCC_ERR_BAD_ARG, "null output");
     if (!c->have_ccsd) fcc::fail(FCC_ERR_STATE, "run CCSD before (T)");
-    if (precision != FCC_PREC_FP64) fcc::fail(FCC_ERR_BAD_ARG, "this build runs FCC_PREC_FP64 (T) only");
-    *et_out = fcc::triples_fp64(c);
+    if (precision != FCC_PREC_FP64 && precision != FCC_PREC_MIXED) fcc::fail(FCC_ERR_BAD_ARG, "bad precision");
+    *et_out = precision == FCC_PREC_FP64 ? fcc::triples_fp64(c) : fcc::triples_mixed(c);
     return std::isfinite(*et_out) ? FCC_OK : FCC_ERR_NAN;
   });
 }

@@ -27,7 +27,14 @@ struct Error {
                   std::string(#call) + ": " + cudaGetErrorString(e__));                         \
   } while (0)
 
-#define FCC_CHECK_LAUNCH() FCC_CUDA(cudaGetLastError())
+// Every kernel launch site is followed by this check, which also counts the
+// launch (the count is exposed for measurement through fcc_stat_launches).
+void note_launch();
+#define FCC_CHECK_LAUNCH()          \
+  do {                              \
+    ::fcc::note_launch();           \
+    FCC_CUDA(cudaGetLastError());   \
+  } while (0)
 
 // Device buffer owned by a context.
 template <class T>

@@ -2,6 +2,7 @@
 // options and the iteration state.
 #pragma once
 #include "fcc_common.cuh"
+#include "fcc_tc.cuh"
 
 struct fcc_ctx {
   int device = 0;
@@ -39,6 +40,12 @@ struct fcc_ctx {
   fcc::DBuf<float> derr1s, derr2s;
   fcc::DBuf<double> derr1d, derr2d;
 
+  // split-BF16 tensor-core engine (mixed form) and its device error flag
+  fcc::TcEngine tc;
+  fcc::DBuf<int> dev_err;
+  // statistics of the last run
+  int64_t launches = 0;
+
   // (T) scratch
   fcc::DBuf<double> ovvv, ooov, Wt;
 };
@@ -47,7 +54,8 @@ namespace fcc {
 void setup_integrals(fcc_ctx* c);
 void make_mp2_guess(fcc_ctx* c);
 double cc_energy(fcc_ctx* c, const double* t1, const double* t2);
-void residual_fp64(fcc_ctx* c);
+void residual(fcc_ctx* c);
 int ccsd_run(fcc_ctx* c, const fcc_opts* opts, fcc_iter_stats* log, int32_t log_cap, fcc_ccsd_result* out);
 double triples_fp64(fcc_ctx* c);
+double triples_mixed(fcc_ctx* c);
 }  // namespace fcc

@@ -16,15 +16,22 @@ struct PackSpec {
 };
 
 // Output scatter of the GEMM: element (m, n) goes to
-// C[m1*ms1 + m2*ms2 + m3*ms3 + n1*ns1 + n2*ns2 + n3*ns3] (FP64 or FP32) as
-// alpha * acc + beta * C.
+// C[m1*ms1 + m2*ms2 + m3*ms3 + n1*ns1 + n2*ns2 + n3*ns3] as
+//   EPI_F64 / EPI_F32: alpha * acc + beta * C (atomic add when split over K);
+//   EPI_SPLIT: bf16 hi/lo of alpha * acc written as three pieces at offsets
+//              0, piece, 2*piece (bit p of `pattern` set = lo), i.e. straight
+//              into the packed operand of a following GEMM.
+enum { EPI_F64 = 0, EPI_F32 = 1, EPI_SPLIT = 2 };
 struct EpiMap {
-  int64_t M, N;
-  int64_t md2, md3, ms1, ms2, ms3;
-  int64_t nd2, nd3, ns1, ns2, ns3;
-  double alpha, beta;
-  void* C;
-  int c_fp32;
+  int64_t M = 0, N = 0;
+  int64_t md2 = 1, md3 = 1, ms1 = 0, ms2 = 0, ms3 = 0;
+  int64_t nd2 = 1, nd3 = 1, ns1 = 0, ns2 = 0, ns3 = 0;
+  double alpha = 1.0, beta = 0.0;
+  void* C = nullptr;
+  int mode = EPI_F64;
+  int atomic = 0;
+  int64_t piece = 0;
+  int pattern = 0;
 };
 
 int64_t packed_kp(int64_t K);
@@ -39,8 +46,8 @@ void gemm_bf16x3(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const _
 // counters of what ran.
 struct TcEngine {
   bool enabled = false;
-  double min_flops = 5e7;
-  int64_t min_dim = 32;   // smallest M and N routed to the tensor cores
+  double min_flops = 1e6;
+  int64_t min_dim = 16;   // smallest M and N routed to the tensor cores
   DBuf<__nv_bfloat16> bufA, bufB;
   int* err = nullptr;
   int64_t tc_calls = 0, f64_calls = 0;

@@ -2,7 +2,9 @@
 #include <cstring>
 
 #include "../../include/fermicc_testing.h"
-#include "fcc_tc.cuh"
+#include "fcc_ctx.cuh"
+
+static cudaStream_t fcc_stream_of(const fcc_ctx* c) { return c->stream; }
 
 namespace {
 
@@ -22,6 +24,12 @@ int64_t count(const int64_t* dims, int rank) {
 }
 
 }  // namespace
+
+namespace fcc { int64_t launch_count(); }
+
+extern "C" int64_t fcc_stat_launches(void) { return fcc::launch_count(); }
+
+extern "C" void* fcc_stream(const fcc_ctx* c) { return c ? (void*)fcc_stream_of(c) : nullptr; }
 
 extern "C" int fcc_test_contract(int32_t precision, const char* spec, const double* A, const int64_t* adims,
                                  int32_t arank, const double* B, const int64_t* bdims, int32_t brank, double* C,

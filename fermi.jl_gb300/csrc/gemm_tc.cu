@@ -100,7 +100,7 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
 template <int BN>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     gemm_bf16_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t a_row0,
-                        int64_t b_row0, int num_k, EpiMap ep, int* err) {
+                        int64_t b_row0, int num_k, int k_chunk, EpiMap ep, int* err) {
   using Cfg = TcCfg<BN>;
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[Cfg::STAGES];
@@ -135,24 +135,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t tmem = tmem_holder;
   const int64_t m0 = (int64_t)blockIdx.x * BM;
   const int64_t n0 = (int64_t)blockIdx.y * BN;
+  // split-K: this CTA reduces k-tiles [kb, ke); partial sums are added atomically
+  const int kb = (int)blockIdx.z * k_chunk;
+  const int ke = min(num_k, kb + k_chunk);
+  const int nkt = max(0, ke - kb);
 
   if (warp == 0 && lane == 0) {
     // ---------------- TMA producer
-    for (int kt = 0; kt < num_k; ++kt) {
+    for (int kt = 0; kt < nkt; ++kt) {
       const int s = kt % Cfg::STAGES;
       const uint32_t ph = (kt / Cfg::STAGES) & 1;
       if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1)) { atomicExch(&abort_flag, 1); break; }
       if (*(volatile int*)&abort_flag) break;
       const uint32_t fb = smem_u32(&full_bar[s]);
       mbar_expect_tx(fb, Cfg::STAGE_BYTES);
-      tma_load_2d(smem_u32(sA + s * Cfg::A_BYTES), &tmA, kt * BK, (int32_t)(a_row0 + m0), fb);
-      tma_load_2d(smem_u32(sB + s * Cfg::B_BYTES), &tmB, kt * BK, (int32_t)(b_row0 + n0), fb);
+      tma_load_2d(smem_u32(sA + s * Cfg::A_BYTES), &tmA, (kb + kt) * BK, (int32_t)(a_row0 + m0), fb);
+      tma_load_2d(smem_u32(sB + s * Cfg::B_BYTES), &tmB, (kb + kt) * BK, (int32_t)(b_row0 + n0), fb);
     }
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer (single thread)
     constexpr uint32_t idesc = idesc_bf16(BM, BN);
     bool ok = true;
-    for (int kt = 0; kt < num_k; ++kt) {
+    for (int kt = 0; kt < nkt; ++kt) {
       const int s = kt % Cfg::STAGES;
       const uint32_t ph = (kt / Cfg::STAGES) & 1;
       if (!mbar_wait(smem_u32(&full_bar[s]), ph)) { atomicExch(&abort_flag, 1); ok = false; break; }
@@ -186,7 +190,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int row = q * 32 + lane;
     const int64_t m = m0 + row;
     const bool abort_now = __any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0);
-    if (ok && !abort_now) {
+    if (ok && !abort_now && nkt > 0) {
       int64_t crow = 0;
       if (m < ep.M) {
         int64_t m3 = m % ep.md3, r = m / ep.md3;
@@ -215,12 +219,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             int64_t n2 = rr % ep.nd2, n1 = rr / ep.nd2;
             const int64_t off = crow + n1 * ep.ns1 + n2 * ep.ns2 + n3 * ep.ns3;
             const double val = ep.alpha * (double)__uint_as_float(r[j]);
-            if (ep.c_fp32) {
+            if (ep.mode == EPI_SPLIT) {
+              __nv_bfloat16* dst = static_cast<__nv_bfloat16*>(ep.C) + off;
+              const float f = __uint_as_float(r[j]) * (float)ep.alpha;
+              const __nv_bfloat16 hi = __float2bfloat16_rn(f);
+              const __nv_bfloat16 lo = __float2bfloat16_rn(f - __bfloat162float(hi));
+              dst[0] = ((ep.pattern >> 0) & 1) ? lo : hi;
+              dst[ep.piece] = ((ep.pattern >> 1) & 1) ? lo : hi;
+              dst[2 * ep.piece] = ((ep.pattern >> 2) & 1) ? lo : hi;
+            } else if (ep.mode == EPI_F32) {
               float* dst = static_cast<float*>(ep.C) + off;
-              *dst = (float)(ep.beta != 0.0 ? val + ep.beta * (double)*dst : val);
+              if (ep.atomic) atomicAdd(dst, (float)val);
+              else *dst = (float)(ep.beta != 0.0 ? val + ep.beta * (double)*dst : val);
             } else {
               double* dst = static_cast<double*>(ep.C) + off;
-              *dst = ep.beta != 0.0 ? val + ep.beta * *dst : val;
+              if (ep.atomic) atomicAdd(dst, val);
+              else *dst = ep.beta != 0.0 ? val + ep.beta * *dst : val;
             }
           }
         }
@@ -237,32 +251,115 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 }
 
 // ---------------------------------------------------------------- packing
-__device__ __forceinline__ void split2(double x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
-  hi = __float2bfloat16_rn((float)x);
-  lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
+
+__device__ __forceinline__ int64_t row_off(const PackSpec& ps, int64_t r) {
+  const int64_t r3 = r % ps.rd3, q = r / ps.rd3;
+  return (q / ps.rd2) * ps.rs1 + (q % ps.rd2) * ps.rs2 + r3 * ps.rs3;
+}
+__device__ __forceinline__ int64_t col_off(const PackSpec& ps, int64_t k) {
+  const int64_t k3 = k % ps.kd3, q = k / ps.kd3;
+  return (q / ps.kd2) * ps.ks1 + (q % ps.kd2) * ps.ks2 + k3 * ps.ks3;
 }
 
 // dst[r][k'] (row pitch Kp) from src: piece p of k' = p*K + k holds hi or lo
 // of src(r, k) per `pattern` (bit p set = lo); columns >= 3K are zero.
-__global__ void pack_split_kernel(const double* __restrict__ src, PackSpec ps, int pattern,
-                                  __nv_bfloat16* __restrict__ dst) {
-  const int64_t total = ps.R * ps.Kp;
+// Row-major walk: each thread splits 4 consecutive k of one row once and
+// writes all three pieces (used when k is the faster source index).
+__global__ void pack_rows_kernel(const double* __restrict__ src, PackSpec ps, int pattern, __nv_bfloat16* __restrict__ dst) {
+  const int64_t kq = (ps.Kp + 3) / 4;   // groups of 4 columns over [0, Kp)
+  const int64_t total = ps.R * kq;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = t / ps.Kp, kk = t - r * ps.Kp;
-    __nv_bfloat16 outv = __float2bfloat16_rn(0.0f);
-    if (kk < 3 * ps.K) {
-      const int piece = (int)(kk / ps.K);
-      const int64_t k = kk - piece * ps.K;
-      int64_t r3 = r % ps.rd3, q = r / ps.rd3;
-      int64_t r2 = q % ps.rd2, r1 = q / ps.rd2;
-      int64_t k3 = k % ps.kd3, q2 = k / ps.kd3;
-      int64_t k2 = q2 % ps.kd2, k1 = q2 / ps.kd2;
-      const double x = src[r1 * ps.rs1 + r2 * ps.rs2 + r3 * ps.rs3 + k1 * ps.ks1 + k2 * ps.ks2 + k3 * ps.ks3];
-      __nv_bfloat16 hi, lo;
-      split2(x, hi, lo);
-      outv = ((pattern >> piece) & 1) ? lo : hi;
+    const int64_t r = t / kq, g = t - r * kq;
+    const int64_t k0 = g * 4;
+    __nv_bfloat16* drow = dst + r * ps.Kp;
+    if (k0 < ps.K) {
+      const int64_t ro = row_off(ps, r);
+      __nv_bfloat16 hi[4], lo[4];
+      const int cnt = (int)min((int64_t)4, ps.K - k0);
+      for (int q = 0; q < 4; ++q) {
+        double x = q < cnt ? src[ro + col_off(ps, k0 + q)] : 0.0;
+        hi[q] = __float2bfloat16_rn((float)x);
+        lo[q] = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi[q])));
+      }
+      for (int p = 0; p < 3; ++p) {
+        const bool use_lo = (pattern >> p) & 1;
+        __nv_bfloat16* d = drow + p * ps.K + k0;
+        if (cnt == 4 && (reinterpret_cast<uintptr_t>(d) & 7) == 0) {
+          __nv_bfloat162 v0 = use_lo ? __halves2bfloat162(lo[0], lo[1]) : __halves2bfloat162(hi[0], hi[1]);
+          __nv_bfloat162 v1 = use_lo ? __halves2bfloat162(lo[2], lo[3]) : __halves2bfloat162(hi[2], hi[3]);
+          uint2 u;
+          u.x = *reinterpret_cast<uint32_t*>(&v0);
+          u.y = *reinterpret_cast<uint32_t*>(&v1);
+          *reinterpret_cast<uint2*>(d) = u;
+        } else {
+          for (int q = 0; q < cnt; ++q) d[q] = use_lo ? lo[q] : hi[q];
+        }
+      }
     }
-    dst[t] = outv;
+    // zero padding [3K, Kp)
+    for (int q = 0; q < 4; ++q) {
+      const int64_t kk = 3 * ps.K + k0 + q;
+      if (k0 + q < ps.Kp - 3 * ps.K && kk < ps.Kp) drow[kk] = __float2bfloat16_rn(0.0f);
+    }
+  }
+}
+
+// Transposing walk through a 32 x 32 shared-memory tile, for sources whose
+// row index is the faster one in memory: reads coalesce along rows, writes
+// along k.
+__global__ void pack_tiles_kernel(const double* __restrict__ src, PackSpec ps, int pattern, __nv_bfloat16* __restrict__ dst) {
+  __shared__ double tile[32][33];
+  const int64_t ntr = (ps.R + 31) / 32, ntk = (ps.K + 31) / 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
+  for (int64_t tb = blockIdx.x; tb < ntr * ntk; tb += gridDim.x) {
+    const int64_t r0 = (tb / ntk) * 32, k0 = (tb % ntk) * 32;
+    __syncthreads();
+    for (int j = 0; j < 4; ++j) {
+      const int kk = ty + 8 * j;
+      const int64_t r = r0 + tx, k = k0 + kk;
+      tile[kk][tx] = (r < ps.R && k < ps.K) ? src[row_off(ps, r) + col_off(ps, k)] : 0.0;
+    }
+    __syncthreads();
+    for (int j = 0; j < 4; ++j) {
+      const int rr = ty + 8 * j;
+      const int64_t r = r0 + rr, k = k0 + tx;
+      if (r >= ps.R || k >= ps.K) continue;
+      const double x = tile[tx][rr];
+      const __nv_bfloat16 hi = __float2bfloat16_rn((float)x);
+      const __nv_bfloat16 lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
+      __nv_bfloat16* d = dst + r * ps.Kp + k;
+      d[0] = (pattern & 1) ? lo : hi;
+      d[ps.K] = (pattern & 2) ? lo : hi;
+      d[2 * ps.K] = (pattern & 4) ? lo : hi;
+    }
+  }
+}
+
+// zero columns [3K, Kp) of every row
+__global__ void pack_pad_kernel(PackSpec ps, __nv_bfloat16* __restrict__ dst) {
+  const int64_t w = ps.Kp - 3 * ps.K;
+  const int64_t total = ps.R * w;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / w, c = t - r * w;
+    dst[r * ps.Kp + 3 * ps.K + c] = __float2bfloat16_rn(0.0f);
+  }
+}
+
+// C = beta * C over an epilogue map (before split-K atomics).
+__global__ void scale_out_kernel(EpiMap ep, double beta) {
+  const int64_t total = ep.M * ep.N;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = t / ep.N, n = t - m * ep.N;
+    const int64_t m3 = m % ep.md3, qm = m / ep.md3, n3 = n % ep.nd3, qn = n / ep.nd3;
+    const int64_t off = (qm / ep.md2) * ep.ms1 + (qm % ep.md2) * ep.ms2 + m3 * ep.ms3 + (qn / ep.nd2) * ep.ns1 +
+                        (qn % ep.nd2) * ep.ns2 + n3 * ep.ns3;
+    if (ep.mode == EPI_F32) {
+      float* d = static_cast<float*>(ep.C) + off;
+      *d = beta == 0.0 ? 0.0f : (float)(beta * *d);
+    } else {
+      double* d = static_cast<double*>(ep.C) + off;
+      *d = beta == 0.0 ? 0.0 : beta * *d;
+    }
   }
 }
 
@@ -308,9 +405,25 @@ void launch_tc(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __n
   });
   CUtensorMap ta = make_map(A, a_rows, Kp, BM);
   CUtensorMap tb = make_map(B, b_rows, Kp, BN);
-  dim3 grid((unsigned)((ep.M + BM - 1) / BM), (unsigned)((ep.N + BN - 1) / BN));
+  const int64_t tm = (ep.M + BM - 1) / BM, tn = (ep.N + BN - 1) / BN;
+  const int num_k = (int)(Kp / BK);
+  // split K across CTAs when the output has too few tiles to fill the GPU
+  int splits = 1;
+  if (ep.mode != EPI_SPLIT && tm * tn < 152 && num_k >= 16)
+    splits = (int)std::min<int64_t>((152 + tm * tn - 1) / (tm * tn), num_k / 8);
+  splits = std::max(1, std::min(splits, 64));
+  const int chunk = (num_k + splits - 1) / splits;
+  splits = (num_k + chunk - 1) / chunk;
+  EpiMap e2 = ep;
+  if (splits > 1) {
+    const int64_t tot = ep.M * ep.N;
+    scale_out_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 152 * 16), 256, 0, s>>>(ep, ep.beta);
+    FCC_CHECK_LAUNCH();
+    e2.atomic = 1;
+  }
+  dim3 grid((unsigned)tm, (unsigned)tn, (unsigned)splits);
   if (grid.y > 65535) fail(FCC_ERR_BAD_ARG, "tensor-core grid too large");
-  gemm_bf16_tc_kernel<BN><<<grid, TC_THREADS, Cfg::SMEM, s>>>(ta, tb, a_row0, b_row0, (int)(Kp / BK), ep, err);
+  gemm_bf16_tc_kernel<BN><<<grid, TC_THREADS, Cfg::SMEM, s>>>(ta, tb, a_row0, b_row0, num_k, chunk, e2, err);
   FCC_CHECK_LAUNCH();
 }
 
@@ -319,13 +432,25 @@ void launch_tc(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __n
 int64_t packed_kp(int64_t K) { return ((3 * K + BK - 1) / BK) * BK; }
 
 void pack_split(const double* src, const PackSpec& ps, bool is_a, __nv_bfloat16* dst, cudaStream_t s) {
-  const int64_t total = ps.R * ps.Kp;
-  if (total <= 0) return;
-  const int threads = 256;
-  const int64_t blocks = std::min<int64_t>((total + threads - 1) / threads, 152 * 64);
+  if (ps.R <= 0 || ps.K <= 0) return;
   // A' = [hi | hi | lo] (lo in piece 2), B' = [hi | lo | hi] (lo in piece 1)
-  pack_split_kernel<<<(unsigned)blocks, threads, 0, s>>>(src, ps, is_a ? 0b100 : 0b010, dst);
-  FCC_CHECK_LAUNCH();
+  const int pattern = is_a ? 0b100 : 0b010;
+  const int64_t kfast = std::llabs(ps.kd3 > 1 ? ps.ks3 : (ps.kd2 > 1 ? ps.ks2 : ps.ks1));
+  const int64_t rfast = std::llabs(ps.rd3 > 1 ? ps.rs3 : (ps.rd2 > 1 ? ps.rs2 : ps.rs1));
+  if (rfast < kfast && ps.R >= 32) {
+    const int64_t tiles = ((ps.R + 31) / 32) * ((ps.K + 31) / 32);
+    pack_tiles_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 16), 256, 0, s>>>(src, ps, pattern, dst);
+    FCC_CHECK_LAUNCH();
+    if (ps.Kp > 3 * ps.K) {
+      const int64_t tot = ps.R * (ps.Kp - 3 * ps.K);
+      pack_pad_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 152 * 16), 256, 0, s>>>(ps, dst);
+      FCC_CHECK_LAUNCH();
+    }
+  } else {
+    const int64_t total = ps.R * ((ps.Kp + 3) / 4);
+    pack_rows_kernel<<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 32), 256, 0, s>>>(src, ps, pattern, dst);
+    FCC_CHECK_LAUNCH();
+  }
 }
 
 void gemm_bf16x3(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __nv_bfloat16* B, int64_t b_rows,

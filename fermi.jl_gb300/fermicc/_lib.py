@@ -27,7 +27,7 @@ FCC_PREC_MIXED = 1
 # every symbol include/fermicc.h declares, and the test hooks of include/fermicc_testing.h
 EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess",
            "fcc_ccsd_run", "fcc_get_amps", "fcc_triples", "fcc_destroy", "fcc_strerror", "fcc_last_error")
-TEST_EXPORTS = ("fcc_test_contract",)
+TEST_EXPORTS = ("fcc_test_contract", "fcc_stat_launches", "fcc_stream")
 
 
 class FccOpts(ctypes.Structure):
@@ -84,6 +84,10 @@ def load():
     lib.fcc_test_contract.argtypes = [i32, ctypes.c_char_p, dp, i64p, i32, dp, i64p, i32, dp, i64p, i32,
                                       ctypes.c_double, ctypes.c_double]
     lib.fcc_test_contract.restype = ctypes.c_int
+    lib.fcc_stat_launches.argtypes = []
+    lib.fcc_stat_launches.restype = ctypes.c_int64
+    lib.fcc_stream.argtypes = [vp]
+    lib.fcc_stream.restype = ctypes.c_void_p
     for name in ("fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess", "fcc_ccsd_run",
                  "fcc_get_amps", "fcc_triples"):
         getattr(lib, name).restype = ctypes.c_int

@@ -46,7 +46,10 @@ extern "C" {
 /* arithmetic of the contractions */
 #define FCC_PREC_FP64 0  /* FP64 throughout (the correctness form)                  */
 #define FCC_PREC_MIXED 1 /* split-BF16 tensor-core contractions, FP32 accumulate,   */
-                         /* FP64 denominators/update/DIIS/energies, FP64 finish    */
+                         /* FP64 denominators/update/DIIS/energies; iterations     */
+                         /* below mixed_switch_rms are corrected by FP64 residual  */
+                         /* evaluations and the run ends on an FP64 residual that  */
+                         /* meets e_conv / max_rms (the FP64 fixed point)          */
 
 typedef struct fcc_ctx fcc_ctx;
 
@@ -70,7 +73,8 @@ typedef struct {
 typedef struct {
   int32_t ite;
   int32_t diis;      /* 1 if this iteration extrapolated                */
-  int32_t precision; /* FCC_PREC_* used for this iteration's residual   */
+  int32_t precision; /* residual of this iteration: 0 FP64, 1 split-BF16, */
+                     /* 2 split-BF16 + FP64 defect correction           */
   int32_t pad;
   double energy;     /* correlation energy after the iteration          */
   double dE;
@@ -110,7 +114,8 @@ int fcc_upload_conv(fcc_ctx* ctx, const double* OOOO, const double* OOOV, const 
                     const double* eps_o, const double* eps_v, double e_ref);
 
 /* Starting amplitudes T1[i,a] (o x v) and T2[i,j,a,b] (o x o x v x v).
- * Without this call the run starts from the MP2 guess. */
+ * Without this call the run starts from the MP2 guess; passing NULL for both
+ * restores the MP2 guess (built on the device). */
 int fcc_set_guess(fcc_ctx* ctx, const double* T1, const double* T2);
 
 /* Run the CCSD iterations.  log may be NULL; otherwise up to log_cap lines are

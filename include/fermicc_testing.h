@@ -22,6 +22,14 @@ int fcc_test_contract(int32_t precision, const char* spec, const double* A, cons
                       const double* B, const int64_t* bdims, int32_t brank, double* C, const int64_t* cdims,
                       int32_t crank, double alpha, double beta);
 
+/* Number of kernels this library has launched in the process so far. */
+int64_t fcc_stat_launches(void);
+
+/* The CUDA stream (cudaStream_t) every call on ctx runs on, so a caller can
+ * bracket library work with its own events. */
+typedef struct fcc_ctx fcc_ctx;
+void* fcc_stream(const fcc_ctx* ctx);
+
 #ifdef __cplusplus
 }
 #endif

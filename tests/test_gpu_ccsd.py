@@ -118,3 +118,17 @@ def test_errors_surface_as_status_codes():
         RCCSD.compute(inp, context=ctx)
     Options.reset()
     ctx.close()
+
+
+@pytest.mark.parametrize("n", [2, 4])
+def test_mixed_form_reaches_the_fp64_fixed_point(n):
+    # split-BF16 iterations until rms < 1e-5, then FP64: same converged energy
+    inp = inputs(n)
+    opt = dict(cc_e_conv=1e-9, cc_max_rms=1e-8)
+    e64 = _gpu_run(inp, **opt)
+    mix = _gpu_run(inp, cc_gpu_precision="mixed", **opt)
+    assert mix.converged
+    precs = [l["precision"] for l in mix.iterations]
+    assert precs[0] == 1 and precs[-1] == 0          # started mixed, finished FP64
+    assert abs(mix.correlation - e64.correlation) < 1e-7
+    assert np.abs(mix.T2 - e64.T2).max() < 1e-6

@@ -19,6 +19,8 @@ CASES = [
     ("lb,lca->abc", (9, 40), (9, 33, 37), (37, 40, 33)),
     ("Qai,Qbj->ijab", (50, 20, 6), (50, 21, 7), (6, 7, 20, 21)),
     ("abd,cd->abc", (17, 19, 150), (300, 150), (17, 19, 300)),
+    ("ikac,kc->ia", (40, 5, 36, 7), (5, 7), (40, 36)),              # N = 1 (matrix-vector)
+    ("jlcd,klcd->kj", (20, 9, 30, 11), (24, 9, 30, 11), (24, 20)),  # few tiles, long K (split-K)
 ]
 
 
