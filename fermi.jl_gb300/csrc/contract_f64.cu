@@ -326,15 +326,16 @@ void run_tc(TcEngine* tc, double alpha, const TView& A, const TView& B, double b
   order(gk, 0);
   pad3(gm); pad3(gn); pad3(gk);
   const int64_t M = gdim(gm), N = gdim(gn), K = gdim(gk);
-  const int64_t Kp = packed_kp(K);
+  const SplitScheme sc = tc->scheme;
+  const int64_t Kp = packed_kp(K, sc.P);
   if ((int64_t)tc->bufA.n < M * Kp) tc->bufA.alloc(M * Kp);
   if ((int64_t)tc->bufB.n < N * Kp) tc->bufB.alloc(N * Kp);
   PackSpec pa{M, K, Kp, gm[1].dim, gm[2].dim, gm[0].s[0], gm[1].s[0], gm[2].s[0],
-              gk[1].dim, gk[2].dim, gk[0].s[0], gk[1].s[0], gk[2].s[0]};
+              gk[1].dim, gk[2].dim, gk[0].s[0], gk[1].s[0], gk[2].s[0], sc.P, sc.code_a};
   PackSpec pb{N, K, Kp, gn[1].dim, gn[2].dim, gn[0].s[1], gn[1].s[1], gn[2].s[1],
-              gk[1].dim, gk[2].dim, gk[0].s[1], gk[1].s[1], gk[2].s[1]};
-  pack_split(A.p, pa, true, tc->bufA.p, s);
-  pack_split(B.p, pb, false, tc->bufB.p, s);
+              gk[1].dim, gk[2].dim, gk[0].s[1], gk[1].s[1], gk[2].s[1], sc.P, sc.code_b};
+  pack_split(A.p, pa, tc->bufA.p, s);
+  pack_split(B.p, pb, tc->bufB.p, s);
   EpiMap ep;
   ep.M = M; ep.N = N;
   ep.md2 = gm[1].dim; ep.md3 = gm[2].dim; ep.ms1 = gm[0].s[2]; ep.ms2 = gm[1].s[2]; ep.ms3 = gm[2].s[2];
@@ -342,7 +343,7 @@ void run_tc(TcEngine* tc, double alpha, const TView& A, const TView& B, double b
   ep.alpha = alpha; ep.beta = beta; ep.C = C.p; ep.mode = EPI_F64;
   gemm_bf16x3(tc->bufA.p, M, 0, tc->bufB.p, N, 0, Kp, ep, tc->err, s);
   tc->tc_calls++;
-  tc->tc_flops += 2.0 * (double)M * (double)N * (double)K;
+  tc->tc_flops += 2.0 * (double)M * (double)N * (double)K * sc.P;
 }
 
 }  // namespace

@@ -6,21 +6,38 @@
 
 namespace fcc {
 
+// Split schemes.  x = hi + mid + lo with hi = bf16(x), mid = bf16(x - hi),
+// lo = bf16(x - hi - mid).  A product A.B is evaluated as a sum of P piece
+// products, stored as P column blocks of the packed operands:
+//   3 products: A' = [hi hi mid],          B' = [hi mid hi]          (~2^-16)
+//   6 products: A' = [hi hi mid hi mid lo], B' = [hi mid hi lo mid hi] (~2^-24)
+// Piece p of an operand holds level (code >> 2p) & 3 (0 hi, 1 mid, 2 lo).
+struct SplitScheme {
+  int P;
+  uint32_t code_a, code_b;
+};
+constexpr SplitScheme SPLIT3{3, 0u | (0u << 2) | (1u << 4), 0u | (1u << 2) | (0u << 4)};
+constexpr SplitScheme SPLIT6{6, 0u | (0u << 2) | (1u << 4) | (0u << 6) | (1u << 8) | (2u << 10),
+                             0u | (1u << 2) | (0u << 4) | (2u << 6) | (1u << 8) | (0u << 10)};
+
 // Gather spec of a packed operand: row r = (r1*rd2 + r2)*rd3 + r3 and column
 // k = (k1*kd2 + k2)*kd3 + k3 of a strided FP64 source; the destination is
-// R rows x Kp bf16 with the three split pieces at columns [0,K), [K,2K), [2K,3K).
+// R rows x Kp bf16 with split piece p at columns [p*K, (p+1)*K), zero from
+// P*K to Kp.
 struct PackSpec {
   int64_t R, K, Kp;
   int64_t rd2, rd3, rs1, rs2, rs3;
   int64_t kd2, kd3, ks1, ks2, ks3;
+  int P = 3;
+  uint32_t code = 0;
 };
 
 // Output scatter of the GEMM: element (m, n) goes to
 // C[m1*ms1 + m2*ms2 + m3*ms3 + n1*ns1 + n2*ns2 + n3*ns3] as
 //   EPI_F64 / EPI_F32: alpha * acc + beta * C (atomic add when split over K);
-//   EPI_SPLIT: bf16 hi/lo of alpha * acc written as three pieces at offsets
-//              0, piece, 2*piece (bit p of `pattern` set = lo), i.e. straight
-//              into the packed operand of a following GEMM.
+//   EPI_SPLIT: the split pieces of alpha * acc written at offsets p * piece
+//              (levels per `code`, P pieces), i.e. straight into the packed
+//              operand of a following GEMM.
 enum { EPI_F64 = 0, EPI_F32 = 1, EPI_SPLIT = 2 };
 struct EpiMap {
   int64_t M = 0, N = 0;
@@ -31,11 +48,12 @@ struct EpiMap {
   int mode = EPI_F64;
   int atomic = 0;
   int64_t piece = 0;
-  int pattern = 0;
+  int P = 3;
+  uint32_t code = 0;
 };
 
-int64_t packed_kp(int64_t K);
-void pack_split(const double* src, const PackSpec& ps, bool is_a, __nv_bfloat16* dst, cudaStream_t s);
+int64_t packed_kp(int64_t K, int P = 3);
+void pack_split(const double* src, const PackSpec& ps, __nv_bfloat16* dst, cudaStream_t s);
 // D = A' B'^T over Kp packed columns; rows a_row0.. of A' (a_rows total) and
 // b_row0.. of B' (b_rows total); err set to 1 if a bounded wait gave up.
 void gemm_bf16x3(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __nv_bfloat16* B, int64_t b_rows,
@@ -46,6 +64,7 @@ void gemm_bf16x3(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const _
 // counters of what ran.
 struct TcEngine {
   bool enabled = false;
+  SplitScheme scheme = SPLIT3;
   double min_flops = 1e6;
   int64_t min_dim = 16;   // smallest M and N routed to the tensor cores
   DBuf<__nv_bfloat16> bufA, bufB;

@@ -54,7 +54,8 @@ extern "C" int fcc_test_contract(int32_t precision, const char* spec, const doub
     FCC_CUDA(cudaMemcpyAsync(dB.p, B, nb * 8, cudaMemcpyHostToDevice, s));
     FCC_CUDA(cudaMemcpyAsync(dC.p, C, nc * 8, cudaMemcpyHostToDevice, s));
     fcc::TcEngine eng;
-    eng.enabled = precision == FCC_PREC_MIXED;
+    eng.enabled = precision != FCC_PREC_FP64;
+    if (precision == 2) eng.scheme = fcc::SPLIT6;
     eng.min_flops = 0.0;
     eng.min_dim = 1;
     eng.err = err.p;
@@ -63,7 +64,7 @@ extern "C" int fcc_test_contract(int32_t precision, const char* spec, const doub
       fcc::einsum(alpha, spec, view_of(dA.p, adims, arank), view_of(dB.p, bdims, brank), beta,
                   view_of(dC.p, cdims, crank), s);
     }
-    if (precision == FCC_PREC_MIXED && eng.tc_calls != 1) return FCC_ERR_BAD_ARG;
+    if (precision != FCC_PREC_FP64 && eng.tc_calls != 1) return FCC_ERR_BAD_ARG;
     int herr = 0;
     FCC_CUDA(cudaMemcpyAsync(C, dC.p, nc * 8, cudaMemcpyDeviceToHost, s));
     FCC_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -97,6 +97,14 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// hi, mid, lo bf16 pieces of x (x - hi - mid - lo ~ 2^-25 |x|)
+__device__ __forceinline__ void split3(double x, __nv_bfloat16 (&lv)[3]) {
+  lv[0] = __float2bfloat16_rn((float)x);
+  const double r = x - (double)__bfloat162float(lv[0]);
+  lv[1] = __float2bfloat16_rn((float)r);
+  lv[2] = __float2bfloat16_rn((float)(r - (double)__bfloat162float(lv[1])));
+}
+
 template <int BN>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     gemm_bf16_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t a_row0,
@@ -108,6 +116,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __shared__ __align__(8) uint64_t acc_bar;
   __shared__ uint32_t tmem_holder;
   __shared__ int abort_flag;
+  __shared__ float epi_tile[4][32][33];   // per epilogue warp: 32 x 32 transpose
 
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* sA = smem;
@@ -191,14 +200,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int64_t m = m0 + row;
     const bool abort_now = __any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0);
     if (ok && !abort_now && nkt > 0) {
+      // this lane's row offset; rows are broadcast to the warp below
       int64_t crow = 0;
       if (m < ep.M) {
         int64_t m3 = m % ep.md3, r = m / ep.md3;
         int64_t m2 = r % ep.md2, m1 = r / ep.md2;
         crow = m1 * ep.ms1 + m2 * ep.ms2 + m3 * ep.ms3;
       }
+      float (*tile)[33] = epi_tile[q];
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 32) {
+        if (n0 + c0 >= ep.N) break;
         uint32_t r[32];
         const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
         asm volatile(
@@ -210,32 +222,40 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (m < ep.M) {
+        // transpose the warp's 32 x 32 block through shared memory so each
+        // store instruction writes 32 consecutive columns of one row
+        __syncwarp();
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int64_t n = n0 + c0 + j;
-            if (n >= ep.N) break;
-            int64_t n3 = n % ep.nd3, rr = n / ep.nd3;
-            int64_t n2 = rr % ep.nd2, n1 = rr / ep.nd2;
-            const int64_t off = crow + n1 * ep.ns1 + n2 * ep.ns2 + n3 * ep.ns3;
-            const double val = ep.alpha * (double)__uint_as_float(r[j]);
-            if (ep.mode == EPI_SPLIT) {
-              __nv_bfloat16* dst = static_cast<__nv_bfloat16*>(ep.C) + off;
-              const float f = __uint_as_float(r[j]) * (float)ep.alpha;
-              const __nv_bfloat16 hi = __float2bfloat16_rn(f);
-              const __nv_bfloat16 lo = __float2bfloat16_rn(f - __bfloat162float(hi));
-              dst[0] = ((ep.pattern >> 0) & 1) ? lo : hi;
-              dst[ep.piece] = ((ep.pattern >> 1) & 1) ? lo : hi;
-              dst[2 * ep.piece] = ((ep.pattern >> 2) & 1) ? lo : hi;
-            } else if (ep.mode == EPI_F32) {
-              float* dst = static_cast<float*>(ep.C) + off;
-              if (ep.atomic) atomicAdd(dst, (float)val);
-              else *dst = (float)(ep.beta != 0.0 ? val + ep.beta * (double)*dst : val);
-            } else {
-              double* dst = static_cast<double*>(ep.C) + off;
-              if (ep.atomic) atomicAdd(dst, val);
-              else *dst = ep.beta != 0.0 ? val + ep.beta * *dst : val;
-            }
+        for (int j = 0; j < 32; ++j) tile[lane][j] = __uint_as_float(r[j]);
+        __syncwarp();
+        const int64_t n = n0 + c0 + lane;
+        const bool nok = n < ep.N;
+        int64_t coff = 0;
+        if (nok) {
+          int64_t n3 = n % ep.nd3, rr = n / ep.nd3;
+          int64_t n2 = rr % ep.nd2, n1 = rr / ep.nd2;
+          coff = n1 * ep.ns1 + n2 * ep.ns2 + n3 * ep.ns3;
+        }
+#pragma unroll 4
+        for (int jr = 0; jr < 32; ++jr) {
+          const int64_t roff = __shfl_sync(0xffffffffu, crow, jr);
+          const int64_t mm = m0 + q * 32 + jr;
+          if (mm >= ep.M || !nok) continue;
+          const int64_t off = roff + coff;
+          const double val = ep.alpha * (double)tile[jr][lane];
+          if (ep.mode == EPI_SPLIT) {
+            __nv_bfloat16* dst = static_cast<__nv_bfloat16*>(ep.C) + off;
+            __nv_bfloat16 lv[3];
+            split3(val, lv);
+            for (int p = 0; p < ep.P; ++p) dst[p * ep.piece] = lv[(ep.code >> (2 * p)) & 3];
+          } else if (ep.mode == EPI_F32) {
+            float* dst = static_cast<float*>(ep.C) + off;
+            if (ep.atomic) atomicAdd(dst, (float)val);
+            else *dst = (float)(ep.beta != 0.0 ? val + ep.beta * (double)*dst : val);
+          } else {
+            double* dst = static_cast<double*>(ep.C) + off;
+            if (ep.atomic) atomicAdd(dst, val);
+            else *dst = ep.beta != 0.0 ? val + ep.beta * *dst : val;
           }
         }
       }
@@ -265,41 +285,38 @@ __device__ __forceinline__ int64_t col_off(const PackSpec& ps, int64_t k) {
 // of src(r, k) per `pattern` (bit p set = lo); columns >= 3K are zero.
 // Row-major walk: each thread splits 4 consecutive k of one row once and
 // writes all three pieces (used when k is the faster source index).
-__global__ void pack_rows_kernel(const double* __restrict__ src, PackSpec ps, int pattern, __nv_bfloat16* __restrict__ dst) {
+__global__ void pack_rows_kernel(const double* __restrict__ src, PackSpec ps, __nv_bfloat16* __restrict__ dst) {
   const int64_t kq = (ps.Kp + 3) / 4;   // groups of 4 columns over [0, Kp)
   const int64_t total = ps.R * kq;
+  const int64_t pk = ps.P * ps.K;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = t / kq, g = t - r * kq;
     const int64_t k0 = g * 4;
     __nv_bfloat16* drow = dst + r * ps.Kp;
     if (k0 < ps.K) {
       const int64_t ro = row_off(ps, r);
-      __nv_bfloat16 hi[4], lo[4];
+      __nv_bfloat16 lv[4][3];
       const int cnt = (int)min((int64_t)4, ps.K - k0);
-      for (int q = 0; q < 4; ++q) {
-        double x = q < cnt ? src[ro + col_off(ps, k0 + q)] : 0.0;
-        hi[q] = __float2bfloat16_rn((float)x);
-        lo[q] = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi[q])));
-      }
-      for (int p = 0; p < 3; ++p) {
-        const bool use_lo = (pattern >> p) & 1;
+      for (int q = 0; q < 4; ++q) split3(q < cnt ? src[ro + col_off(ps, k0 + q)] : 0.0, lv[q]);
+      for (int p = 0; p < ps.P; ++p) {
+        const int lev = (ps.code >> (2 * p)) & 3;
         __nv_bfloat16* d = drow + p * ps.K + k0;
         if (cnt == 4 && (reinterpret_cast<uintptr_t>(d) & 7) == 0) {
-          __nv_bfloat162 v0 = use_lo ? __halves2bfloat162(lo[0], lo[1]) : __halves2bfloat162(hi[0], hi[1]);
-          __nv_bfloat162 v1 = use_lo ? __halves2bfloat162(lo[2], lo[3]) : __halves2bfloat162(hi[2], hi[3]);
+          __nv_bfloat162 v0 = __halves2bfloat162(lv[0][lev], lv[1][lev]);
+          __nv_bfloat162 v1 = __halves2bfloat162(lv[2][lev], lv[3][lev]);
           uint2 u;
           u.x = *reinterpret_cast<uint32_t*>(&v0);
           u.y = *reinterpret_cast<uint32_t*>(&v1);
           *reinterpret_cast<uint2*>(d) = u;
         } else {
-          for (int q = 0; q < cnt; ++q) d[q] = use_lo ? lo[q] : hi[q];
+          for (int q = 0; q < cnt; ++q) d[q] = lv[q][lev];
         }
       }
     }
-    // zero padding [3K, Kp)
+    // zero padding [P*K, Kp)
     for (int q = 0; q < 4; ++q) {
-      const int64_t kk = 3 * ps.K + k0 + q;
-      if (k0 + q < ps.Kp - 3 * ps.K && kk < ps.Kp) drow[kk] = __float2bfloat16_rn(0.0f);
+      const int64_t kk = pk + k0 + q;
+      if (kk < ps.Kp) drow[kk] = __float2bfloat16_rn(0.0f);
     }
   }
 }
@@ -307,7 +324,7 @@ __global__ void pack_rows_kernel(const double* __restrict__ src, PackSpec ps, in
 // Transposing walk through a 32 x 32 shared-memory tile, for sources whose
 // row index is the faster one in memory: reads coalesce along rows, writes
 // along k.
-__global__ void pack_tiles_kernel(const double* __restrict__ src, PackSpec ps, int pattern, __nv_bfloat16* __restrict__ dst) {
+__global__ void pack_tiles_kernel(const double* __restrict__ src, PackSpec ps, __nv_bfloat16* __restrict__ dst) {
   __shared__ double tile[32][33];
   const int64_t ntr = (ps.R + 31) / 32, ntk = (ps.K + 31) / 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
@@ -324,24 +341,21 @@ __global__ void pack_tiles_kernel(const double* __restrict__ src, PackSpec ps, i
       const int rr = ty + 8 * j;
       const int64_t r = r0 + rr, k = k0 + tx;
       if (r >= ps.R || k >= ps.K) continue;
-      const double x = tile[tx][rr];
-      const __nv_bfloat16 hi = __float2bfloat16_rn((float)x);
-      const __nv_bfloat16 lo = __float2bfloat16_rn((float)(x - (double)__bfloat162float(hi)));
+      __nv_bfloat16 lv[3];
+      split3(tile[tx][rr], lv);
       __nv_bfloat16* d = dst + r * ps.Kp + k;
-      d[0] = (pattern & 1) ? lo : hi;
-      d[ps.K] = (pattern & 2) ? lo : hi;
-      d[2 * ps.K] = (pattern & 4) ? lo : hi;
+      for (int p = 0; p < ps.P; ++p) d[p * ps.K] = lv[(ps.code >> (2 * p)) & 3];
     }
   }
 }
 
-// zero columns [3K, Kp) of every row
+// zero columns [P*K, Kp) of every row
 __global__ void pack_pad_kernel(PackSpec ps, __nv_bfloat16* __restrict__ dst) {
-  const int64_t w = ps.Kp - 3 * ps.K;
+  const int64_t w = ps.Kp - ps.P * ps.K;
   const int64_t total = ps.R * w;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = t / w, c = t - r * w;
-    dst[r * ps.Kp + 3 * ps.K + c] = __float2bfloat16_rn(0.0f);
+    dst[r * ps.Kp + ps.P * ps.K + c] = __float2bfloat16_rn(0.0f);
   }
 }
 
@@ -429,26 +443,25 @@ void launch_tc(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __n
 
 }  // namespace
 
-int64_t packed_kp(int64_t K) { return ((3 * K + BK - 1) / BK) * BK; }
+int64_t packed_kp(int64_t K, int P) { return ((P * K + BK - 1) / BK) * BK; }
 
-void pack_split(const double* src, const PackSpec& ps, bool is_a, __nv_bfloat16* dst, cudaStream_t s) {
+void pack_split(const double* src, const PackSpec& ps, __nv_bfloat16* dst, cudaStream_t s) {
   if (ps.R <= 0 || ps.K <= 0) return;
-  // A' = [hi | hi | lo] (lo in piece 2), B' = [hi | lo | hi] (lo in piece 1)
-  const int pattern = is_a ? 0b100 : 0b010;
+  if (ps.P < 1 || ps.P > 8 || ps.Kp < ps.P * ps.K) fail(FCC_ERR_BAD_ARG, "bad pack spec");
   const int64_t kfast = std::llabs(ps.kd3 > 1 ? ps.ks3 : (ps.kd2 > 1 ? ps.ks2 : ps.ks1));
   const int64_t rfast = std::llabs(ps.rd3 > 1 ? ps.rs3 : (ps.rd2 > 1 ? ps.rs2 : ps.rs1));
   if (rfast < kfast && ps.R >= 32) {
     const int64_t tiles = ((ps.R + 31) / 32) * ((ps.K + 31) / 32);
-    pack_tiles_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 16), 256, 0, s>>>(src, ps, pattern, dst);
+    pack_tiles_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 16), 256, 0, s>>>(src, ps, dst);
     FCC_CHECK_LAUNCH();
-    if (ps.Kp > 3 * ps.K) {
-      const int64_t tot = ps.R * (ps.Kp - 3 * ps.K);
+    if (ps.Kp > ps.P * ps.K) {
+      const int64_t tot = ps.R * (ps.Kp - ps.P * ps.K);
       pack_pad_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 152 * 16), 256, 0, s>>>(ps, dst);
       FCC_CHECK_LAUNCH();
     }
   } else {
     const int64_t total = ps.R * ((ps.Kp + 3) / 4);
-    pack_rows_kernel<<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 32), 256, 0, s>>>(src, ps, pattern, dst);
+    pack_rows_kernel<<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 32), 256, 0, s>>>(src, ps, dst);
     FCC_CHECK_LAUNCH();
   }
 }

@@ -8,13 +8,15 @@
 // operand is split and packed once per (T) call into the row layouts the
 // GEMMs read with 2-D TMA boxes:
 //   OVp[x][y][z][d]   = (xy|zd)         (A and B patterns)
+//   OVpT[x][y][z][d]  = (xz|yd)         (B)
 //   P1[x][k][c][d]    = t(k,x,c,d)      (B)
-//   P2[x][k][b][d]    = t(x,k,b,d)      (A and B)
-//   P3[x][c][a][l]    = t(x,l,c,a)      (B)
+//   P2[x][k][b][d]    = t(x,k,b,d)      (A)
+//   P3[x][c][a][l]    = t(x,l,c,a)      (A and B)
+//   P3T[x][y][z][l]   = t(x,l,z,y)      (B)
 //   OOq[x][y][a][l]   = (ly|xa)         (A)
-//   OOr[y][x][a][l]   = (ly|xa)         (A)
+//   OOr[y][x][a][l]   = (ly|xa)         (B)
 // and each GEMM's epilogue scatters into W[k][a][b][c] (FP32) with the index
-// permutation of its term.
+// permutation of its term; every GEMM is oriented so its N index ends in c.
 #include <cmath>
 
 #include "fcc_ctx.cuh"
@@ -100,7 +102,9 @@ PackSpec pspec(int64_t d1, int64_t d2, int64_t d3, int64_t s1, int64_t s2, int64
   PackSpec p;
   p.R = d1 * d2 * d3;
   p.K = K;
-  p.Kp = packed_kp(K);
+  p.Kp = packed_kp(K, SPLIT3.P);
+  p.P = SPLIT3.P;
+  p.code = SPLIT3.code_a;
   p.rd2 = d2; p.rd3 = d3; p.rs1 = s1; p.rs2 = s2; p.rs3 = s3;
   p.kd2 = 1; p.kd3 = K; p.ks1 = 0; p.ks2 = 0; p.ks3 = ks;
   return p;
@@ -132,28 +136,34 @@ double triples_mixed(fcc_ctx* c) {
   einsum(1.0, "Qia,Qbd->iabd", Bov, Bvv, 0.0, rm(ovvv.p, {o, v, v, v}), s);
   einsum(1.0, "Qli,Qjb->lijb", Boo, Bov, 0.0, rm(ooov.p, {o, o, o, v}), s);
   const int64_t v2 = v * v, v3 = v2 * v;
-  const int64_t Kv = packed_kp(v), Ko = packed_kp(o);
-  DBuf<__nv_bfloat16> OVpA, OVpB, P1, P2A, P2B, P3, OOq, OOr;
-  PackSpec ps_ov = pspec(o, v, v, v3, v2, v, v, 1);
-  OVpA.alloc(ps_ov.R * Kv); OVpB.alloc(ps_ov.R * Kv);
-  pack_split(ovvv.p, ps_ov, true, OVpA.p, s);
-  pack_split(ovvv.p, ps_ov, false, OVpB.p, s);
+  const int64_t Kv = packed_kp(v, SPLIT3.P), Ko = packed_kp(o, SPLIT3.P);
+  auto packA = [&](const double* src, PackSpec ps, __nv_bfloat16* dst) { ps.code = SPLIT3.code_a; pack_split(src, ps, dst, s); };
+  auto packB = [&](const double* src, PackSpec ps, __nv_bfloat16* dst) { ps.code = SPLIT3.code_b; pack_split(src, ps, dst, s); };
+  DBuf<__nv_bfloat16> OVpA, OVpB, OVpTB, P1, P2A, P3, P3A, P3T, OOq, OOrB;
+  PackSpec ps_ov = pspec(o, v, v, v3, v2, v, v, 1);            // OVp[x][y][z]  = (xy|zd)
+  PackSpec ps_ovt = pspec(o, v, v, v3, v, v2, v, 1);           // OVpT[x][y][z] = (xz|yd)
+  OVpA.alloc(ps_ov.R * Kv); OVpB.alloc(ps_ov.R * Kv); OVpTB.alloc(ps_ovt.R * Kv);
+  packA(ovvv.p, ps_ov, OVpA.p);
+  packB(ovvv.p, ps_ov, OVpB.p);
+  packB(ovvv.p, ps_ovt, OVpTB.p);
   ovvv.release();
   const double* t2 = c->t2.p;   // t2[i][j][a][b]: strides o*v2, v2, v, 1
-  PackSpec ps1 = pspec(o, o, v, v2, o * v2, v, v, 1);          // P1[x][k][c] = t(k,x,c,:)
-  PackSpec ps2 = pspec(o, o, v, o * v2, v2, v, v, 1);          // P2[x][k][b] = t(x,k,b,:)
-  PackSpec ps3 = pspec(o, v, v, o * v2, v, 1, o, v2);          // P3[x][c][a] over l = t(x,l,c,a)
-  P1.alloc(ps1.R * Kv); P2A.alloc(ps2.R * Kv); P2B.alloc(ps2.R * Kv); P3.alloc(ps3.R * Ko);
-  pack_split(t2, ps1, false, P1.p, s);
-  pack_split(t2, ps2, true, P2A.p, s);
-  pack_split(t2, ps2, false, P2B.p, s);
-  pack_split(t2, ps3, false, P3.p, s);
+  PackSpec ps1 = pspec(o, o, v, v2, o * v2, v, v, 1);          // P1[x][k][c]  = t(k,x,c,:)
+  PackSpec ps2 = pspec(o, o, v, o * v2, v2, v, v, 1);          // P2[x][k][b]  = t(x,k,b,:)
+  PackSpec ps3 = pspec(o, v, v, o * v2, v, 1, o, v2);          // P3[x][c][a]  = t(x,l,c,a) over l
+  PackSpec ps3t = pspec(o, v, v, o * v2, 1, v, o, v2);         // P3T[x][y][z] = t(x,l,z,y) over l
+  P1.alloc(ps1.R * Kv); P2A.alloc(ps2.R * Kv); P3.alloc(ps3.R * Ko); P3A.alloc(ps3.R * Ko); P3T.alloc(ps3t.R * Ko);
+  packB(t2, ps1, P1.p);
+  packA(t2, ps2, P2A.p);
+  packB(t2, ps3, P3.p);
+  packA(t2, ps3, P3A.p);
+  packB(t2, ps3t, P3T.p);
   // ooov[l][y][x][a] = (ly|xa): strides l o2v, y o v, x v, a 1
   PackSpec psq = pspec(o, o, v, v, o * v, 1, o, o * o * v);    // OOq[x][y][a]
   PackSpec psr = pspec(o, o, v, o * v, v, 1, o, o * o * v);    // OOr[y][x][a]
-  OOq.alloc(psq.R * Ko); OOr.alloc(psr.R * Ko);
-  pack_split(ooov.p, psq, true, OOq.p, s);
-  pack_split(ooov.p, psr, true, OOr.p, s);
+  OOq.alloc(psq.R * Ko); OOrB.alloc(psr.R * Ko);
+  packA(ooov.p, psq, OOq.p);
+  packB(ooov.p, psr, OOrB.p);
   ooov.release();
 
   DBuf<float> Wb;
@@ -170,37 +180,38 @@ double triples_mixed(fcc_ctx* c) {
   for (int64_t i = 0; i < o; ++i)
     for (int64_t j = 0; j <= i; ++j) {
       const int64_t nk = j + 1;
-      // W[k][a][b][c]: strides v3, v2, v, 1
+      // W[k][a][b][c]: strides v3, v2, v, 1.  Operands are oriented so the
+      // GEMM's N index ends in c (stride 1): coalesced epilogue stores.
       // :109  (ia|bd) t(k,j,c,d)  -  (li|jb) t(k,l,c,a)
       gemm_bf16x3(OVpA.p, Rov, i * v2, P1.p, Rp, j * o * v, Kv,
                   emap(v2, v, v, 0, v2, v, nk * v, nk, v, 0, v3, 1, 1.0, 0.0, W), err, s);
-      gemm_bf16x3(OOq.p, Rp, (j * o + i) * v, P3.p, Rp3, 0, Ko,
-                  emap(v, 1, v, 0, 0, v, nk * v2, v, v, v3, 1, v2, -1.0, 1.0, W), err, s);
+      gemm_bf16x3(OOq.p, Rp, (j * o + i) * v, P3T.p, Rp3, 0, Ko,
+                  emap(v, 1, v, 0, 0, v, nk * v2, v, v, v3, v2, 1, -1.0, 1.0, W), err, s);
       // :110  (jb|ad) t(k,i,c,d)  -  (lj|ia) t(k,l,c,b)
       gemm_bf16x3(OVpA.p, Rov, j * v2, P1.p, Rp, i * o * v, Kv,
                   emap(v2, v, v, 0, v, v2, nk * v, nk, v, 0, v3, 1, 1.0, 1.0, W), err, s);
-      gemm_bf16x3(OOq.p, Rp, (i * o + j) * v, P3.p, Rp3, 0, Ko,
-                  emap(v, 1, v, 0, 0, v2, nk * v2, v, v, v3, 1, v, -1.0, 1.0, W), err, s);
+      gemm_bf16x3(OOq.p, Rp, (i * o + j) * v, P3T.p, Rp3, 0, Ko,
+                  emap(v, 1, v, 0, 0, v2, nk * v2, v, v, v3, v, 1, -1.0, 1.0, W), err, s);
       // :111  (kc|ad) t(j,i,b,d)  -  (lk|ia) t(j,l,b,c)
-      gemm_bf16x3(P2A.p, Rp, (j * o + i) * v, OVpB.p, Rov, 0, Kv,
-                  emap(v, 1, v, 0, 0, v, nk * v2, v, v, v3, 1, v2, 1.0, 1.0, W), err, s);
+      gemm_bf16x3(P2A.p, Rp, (j * o + i) * v, OVpTB.p, Rov, 0, Kv,
+                  emap(v, 1, v, 0, 0, v, nk * v2, v, v, v3, v2, 1, 1.0, 1.0, W), err, s);
       gemm_bf16x3(OOq.p, Rp, i * o * v, P3.p, Rp3, j * v2, Ko,
                   emap(nk * v, nk, v, 0, v3, v2, v2, v, v, 0, v, 1, -1.0, 1.0, W), err, s);
       // :112  (kc|bd) t(j,i,d,a)  -  (lk|jb) t(i,l,a,c)
-      gemm_bf16x3(P2A.p, Rp, (i * o + j) * v, OVpB.p, Rov, 0, Kv,
-                  emap(v, 1, v, 0, 0, v2, nk * v2, v, v, v3, 1, v, 1.0, 1.0, W), err, s);
+      gemm_bf16x3(P2A.p, Rp, (i * o + j) * v, OVpTB.p, Rov, 0, Kv,
+                  emap(v, 1, v, 0, 0, v2, nk * v2, v, v, v3, v, 1, 1.0, 1.0, W), err, s);
       gemm_bf16x3(OOq.p, Rp, j * o * v, P3.p, Rp3, i * v2, Ko,
                   emap(nk * v, nk, v, 0, v3, v, v2, v, v, 0, v2, 1, -1.0, 1.0, W), err, s);
       // :113  (ia|cd) t(k,j,d,b)  -  (li|kc) t(j,l,b,a)
-      gemm_bf16x3(OVpA.p, Rov, i * v2, P2B.p, Rp, j * o * v, Kv,
-                  emap(v2, v, v, 0, v2, 1, nk * v, nk, v, 0, v3, v, 1.0, 1.0, W), err, s);
-      gemm_bf16x3(OOr.p, Rp, i * o * v, P3.p, Rp3, j * v2, Ko,
-                  emap(nk * v, nk, v, 0, v3, 1, v2, v, v, 0, v, v2, -1.0, 1.0, W), err, s);
+      gemm_bf16x3(P2A.p, Rp, j * o * v, OVpB.p, Rov, i * v2, Kv,
+                  emap(nk * v, nk, v, 0, v3, v, v2, v, v, 0, v2, 1, 1.0, 1.0, W), err, s);
+      gemm_bf16x3(P3A.p, Rp3, j * v2, OOrB.p, Rp, i * o * v, Ko,
+                  emap(v2, v, v, 0, v, v2, nk * v, nk, v, 0, v3, 1, -1.0, 1.0, W), err, s);
       // :114  (jb|cd) t(k,i,d,a)  -  (lj|kc) t(i,l,a,b)
-      gemm_bf16x3(OVpA.p, Rov, j * v2, P2B.p, Rp, i * o * v, Kv,
-                  emap(v2, v, v, 0, v, 1, nk * v, nk, v, 0, v3, v2, 1.0, 1.0, W), err, s);
-      gemm_bf16x3(OOr.p, Rp, j * o * v, P3.p, Rp3, i * v2, Ko,
-                  emap(nk * v, nk, v, 0, v3, 1, v2, v, v, 0, v2, v, -1.0, 1.0, W), err, s);
+      gemm_bf16x3(P2A.p, Rp, i * o * v, OVpB.p, Rov, j * v2, Kv,
+                  emap(nk * v, nk, v, 0, v3, v2, v2, v, v, 0, v, 1, 1.0, 1.0, W), err, s);
+      gemm_bf16x3(P3A.p, Rp3, i * v2, OOrB.p, Rp, j * o * v, Ko,
+                  emap(v2, v, v, 0, v2, v, nk * v, nk, v, 0, v3, 1, -1.0, 1.0, W), err, s);
       dim3 g(EBLOCKS, (unsigned)nk);
       triples_energy_batch_kernel<<<g, EB, 0, s>>>(W, c->t1.p, c->ovov.p, c->eps.p, (int)o, (int)v, (int)i, (int)j,
                                                    part.p);

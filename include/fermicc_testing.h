@@ -16,8 +16,9 @@ extern "C" {
 
 /* C = alpha * einsum(spec, A, B) + beta * C on device 0 for row-major host
  * tensors (rank <= 4 each).  precision FCC_PREC_FP64 runs the DMMA kernel;
- * FCC_PREC_MIXED forces the split-BF16 tensor-core kernel (error if the
- * contraction cannot be expressed for it).  Returns an fcc status code. */
+ * FCC_PREC_MIXED forces the three-product split-BF16 tensor-core kernel and
+ * 2 the six-product one (error if the contraction cannot be expressed for
+ * it).  Returns an fcc status code. */
 int fcc_test_contract(int32_t precision, const char* spec, const double* A, const int64_t* adims, int32_t arank,
                       const double* B, const int64_t* bdims, int32_t brank, double* C, const int64_t* cdims,
                       int32_t crank, double alpha, double beta);

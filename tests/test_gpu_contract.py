@@ -59,3 +59,15 @@ def test_split_bf16_tensor_core_contraction(spec, sa, sb, sc):
     assert rc == 0
     ref2 = -0.5 * ref + 2.0 * C
     assert np.abs(out2 - ref2).max() / np.abs(ref2).max() < 3e-5
+
+
+@pytest.mark.parametrize("spec,sa,sb,sc", CASES)
+def test_six_product_split_contraction(spec, sa, sb, sc):
+    # hi/mid/lo pieces, six products: error ~2^-24 (FP32 accumulation)
+    rng = np.random.default_rng(2)
+    A, B, C = rng.standard_normal(sa), rng.standard_normal(sb), rng.standard_normal(sc)
+    rc, out = _run(2, spec, A, B, C, 1.0, 0.0)
+    assert rc == 0
+    ref = np.einsum(spec, A, B)
+    err = np.abs(out - ref).max() / np.abs(ref).max()
+    assert err < 6e-6, err
