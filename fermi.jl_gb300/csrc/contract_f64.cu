@@ -31,7 +31,8 @@ __device__ __forceinline__ void dmma884(double& d0, double& d1, double a, double
 __global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restrict__ A,
                                                           const double* __restrict__ B,
                                                           double* __restrict__ C, CtrDesc d,
-                                                          int a_mfast, int b_nfast) {
+                                                          int a_mfast, int b_nfast, int64_t k_chunk,
+                                                          double* __restrict__ partial) {
   __shared__ double As[BK][LDS];
   __shared__ double Bs[BK][LDS];
   __shared__ int64_t rowA[BM], colB[BN];
@@ -40,7 +41,10 @@ __global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restri
   const int tid = threadIdx.x;
   const int64_t m0 = (int64_t)blockIdx.x * BM;
   const int64_t n0 = (int64_t)blockIdx.y * BN;
-  const int64_t bz = blockIdx.z;
+  // blockIdx.z: batch index, or the K slice when split over K (partial != 0)
+  const int64_t bz = partial ? 0 : blockIdx.z;
+  const int64_t kbeg = partial ? (int64_t)blockIdx.z * k_chunk : 0;
+  const int64_t kend = partial ? min(d.K, kbeg + k_chunk) : d.K;
   A += bz * d.a_b;
   B += bz * d.b_b;
   C += bz * d.c_b;
@@ -69,7 +73,7 @@ __global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restri
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
 
-  for (int64_t k0 = 0; k0 < d.K; k0 += BK) {
+  for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
     // ---- stage A (BM x BK) and B (BK x BN) into shared memory
     if (a_mfast) {
       int m = tid & 63, kb = tid >> 6;
@@ -78,7 +82,7 @@ __global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restri
         int kk = kb + 2 * r;
         int64_t k = k0 + kk;
         double v = 0.0;
-        if (rowOK[m] && k < d.K) {
+        if (rowOK[m] && k < kend) {
           int64_t k1 = k / d.K2, k2 = k - k1 * d.K2;
           v = A[rowA[m] + k1 * d.a_k1 + k2 * d.a_k2];
         }
@@ -87,7 +91,7 @@ __global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restri
     } else {
       int kk = tid & 15, mb = tid >> 4;
       int64_t k = k0 + kk;
-      bool kok = k < d.K;
+      bool kok = k < kend;
       int64_t koff = 0;
       if (kok) {
         int64_t k1 = k / d.K2, k2 = k - k1 * d.K2;
@@ -106,7 +110,7 @@ __global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restri
         int kk = kb + 2 * r;
         int64_t k = k0 + kk;
         double v = 0.0;
-        if (colOK[n] && k < d.K) {
+        if (colOK[n] && k < kend) {
           int64_t k1 = k / d.K2, k2 = k - k1 * d.K2;
           v = B[colB[n] + k1 * d.b_k1 + k2 * d.b_k2];
         }
@@ -115,7 +119,7 @@ __global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restri
     } else {
       int kk = tid & 15, nb = tid >> 4;
       int64_t k = k0 + kk;
-      bool kok = k < d.K;
+      bool kok = k < kend;
       int64_t koff = 0;
       if (kok) {
         int64_t k1 = k / d.K2, k2 = k - k1 * d.K2;
@@ -158,6 +162,10 @@ __global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restri
       for (int h = 0; h < 2; ++h) {
         int64_t n = n0 + wn + 8 * j + 2 * (lane & 3) + h;
         if (n >= d.N) continue;
+        if (partial) {   // split-K: raw partial sums, reduced in a fixed order later
+          partial[((int64_t)blockIdx.z * d.M + m) * d.N + n] = acc[i][j][h];
+          continue;
+        }
         int64_t n1 = n / d.N2, n2 = n - n1 * d.N2;
         double* dst = C + crow + n1 * d.c_n1 + n2 * d.c_n2;
         double v = d.alpha * acc[i][j][h];
@@ -165,6 +173,22 @@ __global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restri
         *dst = v;
       }
     }
+  }
+}
+
+// C = alpha * sum_z partial[z] + beta * C, summed in slice order.
+__global__ void splitk_reduce_kernel(const double* __restrict__ partial, int splits, double* __restrict__ C,
+                                     CtrDesc d) {
+  const int64_t MN = d.M * d.N;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < MN; t += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int z = 0; z < splits; ++z) s += partial[(int64_t)z * MN + t];
+    const int64_t m = t / d.N, n = t - m * d.N;
+    const int64_t m1 = m / d.M2, m2 = m - m1 * d.M2, n1 = n / d.N2, n2 = n - n1 * d.N2;
+    double* dst = C + m1 * d.c_m1 + m2 * d.c_m2 + n1 * d.c_n1 + n2 * d.c_n2;
+    double v = d.alpha * s;
+    if (d.beta != 0.0) v += d.beta * *dst;
+    *dst = v;
   }
 }
 
@@ -227,8 +251,27 @@ void contract_f64_launch(const double* A, const double* B, double* C, const CtrD
     FCC_CHECK_LAUNCH();
     return;
   }
+  // few output tiles and a long K: split K over CTAs (partials reduced in a
+  // fixed order, so results stay deterministic)
+  if (d.batch == 1 && gm * gn < 152 && d.K >= 32 * BK) {
+    int64_t splits = std::min<int64_t>((2 * 152 + gm * gn - 1) / (gm * gn), d.K / (8 * BK));
+    splits = std::max<int64_t>(2, std::min<int64_t>(splits, 1024));
+    const int64_t chunk = ((d.K + splits - 1) / splits + BK - 1) / BK * BK;
+    splits = (d.K + chunk - 1) / chunk;
+    static thread_local DBuf<double> scratch;
+    const int64_t need = splits * d.M * d.N;
+    if ((int64_t)scratch.n < need) scratch.alloc(need);
+    dim3 grid((unsigned)gm, (unsigned)gn, (unsigned)splits);
+    contract_f64_kernel<<<grid, NT, 0, s>>>(A, B, C, d, d.a_m2 == 1 ? 1 : 0, d.b_n2 == 1 ? 1 : 0, chunk, scratch.p);
+    FCC_CHECK_LAUNCH();
+    const int64_t MN = d.M * d.N;
+    splitk_reduce_kernel<<<(unsigned)std::min<int64_t>((MN + 255) / 256, 152 * 8), 256, 0, s>>>(scratch.p, (int)splits,
+                                                                                                 C, d);
+    FCC_CHECK_LAUNCH();
+    return;
+  }
   dim3 grid((unsigned)gm, (unsigned)gn, (unsigned)d.batch);
-  contract_f64_kernel<<<grid, NT, 0, s>>>(A, B, C, d, d.a_m2 == 1 ? 1 : 0, d.b_n2 == 1 ? 1 : 0);
+  contract_f64_kernel<<<grid, NT, 0, s>>>(A, B, C, d, d.a_m2 == 1 ? 1 : 0, d.b_n2 == 1 ? 1 : 0, d.K, nullptr);
   FCC_CHECK_LAUNCH();
 }
 

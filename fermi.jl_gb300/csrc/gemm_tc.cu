@@ -236,13 +236,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           int64_t n2 = rr % ep.nd2, n1 = rr / ep.nd2;
           coff = n1 * ep.ns1 + n2 * ep.ns2 + n3 * ep.ns3;
         }
-#pragma unroll 4
+        // all loads of the block first (independent, so they overlap), then
+        // the stores
+        const bool rmw = ep.beta != 0.0 && !ep.atomic && ep.mode != EPI_SPLIT;
+        double prev[32];
+        float prevf[32];
+        if (rmw) {
+#pragma unroll
+          for (int jr = 0; jr < 32; ++jr) {
+            const int64_t roff = __shfl_sync(0xffffffffu, crow, jr);
+            const bool ok2 = nok && (m0 + q * 32 + jr) < ep.M;
+            prev[jr] = 0.0;
+            prevf[jr] = 0.0f;
+            if (ok2) {
+              if (ep.mode == EPI_F32) prevf[jr] = static_cast<const float*>(ep.C)[roff + coff];
+              else prev[jr] = static_cast<const double*>(ep.C)[roff + coff];
+            }
+          }
+        }
+#pragma unroll
         for (int jr = 0; jr < 32; ++jr) {
           const int64_t roff = __shfl_sync(0xffffffffu, crow, jr);
           const int64_t mm = m0 + q * 32 + jr;
           if (mm >= ep.M || !nok) continue;
           const int64_t off = roff + coff;
-          const double val = ep.alpha * (double)tile[jr][lane];
+          if (ep.mode == EPI_F32) {
+            // FP32 output: FP32 arithmetic (the FP64 pipe is 1/64 rate on GB300)
+            float* dst = static_cast<float*>(ep.C) + off;
+            float fv = (float)ep.alpha * tile[jr][lane];
+            if (rmw) fv += (float)ep.beta * prevf[jr];
+            if (ep.atomic) atomicAdd(dst, fv);
+            else *dst = fv;
+            continue;
+          }
+          double val = (double)((float)ep.alpha * tile[jr][lane]);
+          if (rmw) val = (ep.beta == 1.0) ? prev[jr] + val : val + ep.beta * prev[jr];
           if (ep.mode == EPI_SPLIT) {
             __nv_bfloat16* dst = static_cast<__nv_bfloat16*>(ep.C) + off;
             __nv_bfloat16 lv[3];
@@ -251,11 +279,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           } else if (ep.mode == EPI_F32) {
             float* dst = static_cast<float*>(ep.C) + off;
             if (ep.atomic) atomicAdd(dst, (float)val);
-            else *dst = (float)(ep.beta != 0.0 ? val + ep.beta * (double)*dst : val);
+            else *dst = (float)val;
           } else {
             double* dst = static_cast<double*>(ep.C) + off;
             if (ep.atomic) atomicAdd(dst, val);
-            else *dst = ep.beta != 0.0 ? val + ep.beta * *dst : val;
+            else *dst = val;
           }
         }
       }

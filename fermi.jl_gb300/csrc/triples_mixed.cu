@@ -1,5 +1,6 @@
 // RCCSD(T) in the mixed form: split-BF16 tensor-core contractions with FP32
-// accumulation for W, FP64 for V's T1 terms, the denominators and the energy.
+// accumulation for W; V and the permutation sums in FP32; the denominators,
+// the division and the energy reduction in FP64.
 //
 // Same algorithm as the FP64 form (PerturbativeTriples/ijk.jl:20-149), batched
 // for the tensor cores: for every pair i >= j the intermediates W_k for all
@@ -33,27 +34,30 @@ __device__ __forceinline__ double warp_sum(double x) {
   return x;
 }
 
-// Energy of the triplets (i, j, k), k = 0..nk-1, from W[k][a][b][c] (FP32);
-// V is formed on the fly with FP64 T1 and (ia|jb).  part[k*EBLOCKS + block]
-// accumulates across calls (fixed summation order).
+// Energy of the triplets (i, j, k), k = 0..nk-1, from W[k][a][b][c] (FP32).
+// V = W + t1_ia (jb|kc) + (ia|kc) t1_jb + (ia|jb) t1_kc and the six-fold
+// permutation sums are FP32 (W itself is an FP32-accumulated split-BF16
+// result); the orbital-energy denominators, the division and the reduction
+// are FP64.  part[k*gridDim.x + block] accumulates across calls in a fixed
+// order.
 __global__ void __launch_bounds__(EB) triples_energy_batch_kernel(const float* __restrict__ Wb,
-                                                                  const double* __restrict__ t1,
-                                                                  const double* __restrict__ ovov,
+                                                                  const float* __restrict__ t1f,
+                                                                  const float* __restrict__ ovovf,
                                                                   const double* __restrict__ eps, int o, int v,
                                                                   int i, int j, double* part) {
   const int k = blockIdx.y;
   if (i == j && j == k) return;
   const float* W = Wb + (int64_t)k * v * v * v;
   const int64_t mstr = (int64_t)o * v;
-  const double* Mjk = ovov + ((int64_t)j * v * o + k) * v;
-  const double* Mik = ovov + ((int64_t)i * v * o + k) * v;
-  const double* Mij = ovov + ((int64_t)i * v * o + j) * v;
-  const double* t1i = t1 + (int64_t)i * v;
-  const double* t1j = t1 + (int64_t)j * v;
-  const double* t1k = t1 + (int64_t)k * v;
-  auto Wat = [&](int x, int y, int z) -> double { return (double)W[((int64_t)x * v + y) * v + z]; };
-  auto Vat = [&](int x, int y, int z) -> double {
-    return Wat(x, y, z) + t1i[x] * Mjk[(int64_t)y * mstr + z] + Mik[(int64_t)x * mstr + z] * t1j[y] +
+  const float* Mjk = ovovf + ((int64_t)j * v * o + k) * v;
+  const float* Mik = ovovf + ((int64_t)i * v * o + k) * v;
+  const float* Mij = ovovf + ((int64_t)i * v * o + j) * v;
+  const float* t1i = t1f + (int64_t)i * v;
+  const float* t1j = t1f + (int64_t)j * v;
+  const float* t1k = t1f + (int64_t)k * v;
+  auto Wat = [&](int x, int y, int z) -> float { return W[((int64_t)x * v + y) * v + z]; };
+  auto Vat = [&](int x, int y, int z, float w) -> float {
+    return w + t1i[x] * Mjk[(int64_t)y * mstr + z] + Mik[(int64_t)x * mstr + z] * t1j[y] +
            Mij[(int64_t)x * mstr + y] * t1k[z];
   };
   const double Dijk = eps[i] + eps[j] + eps[k];
@@ -61,21 +65,22 @@ __global__ void __launch_bounds__(EB) triples_energy_batch_kernel(const float* _
   const int64_t npair = (int64_t)v * (v + 1) / 2;
   double acc = 0.0;
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npair; p += (int64_t)gridDim.x * blockDim.x) {
-    int a = (int)((sqrt(8.0 * (double)p + 1.0) - 1.0) * 0.5);
+    int a = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
     while ((int64_t)a * (a + 1) / 2 > p) --a;
     while ((int64_t)(a + 1) * (a + 2) / 2 <= p) ++a;
     const int b = (int)(p - (int64_t)a * (a + 1) / 2);
     const double Dab = Dijk - fv[a] - fv[b];
     for (int c = 0; c <= b; ++c) {
-      double Wabc = Wat(a, b, c), Wacb = Wat(a, c, b), Wbac = Wat(b, a, c);
-      double Wbca = Wat(b, c, a), Wcab = Wat(c, a, b), Wcba = Wat(c, b, a);
-      double Vabc = Vat(a, b, c), Vacb = Vat(a, c, b), Vbac = Vat(b, a, c);
-      double Vbca = Vat(b, c, a), Vcab = Vat(c, a, b), Vcba = Vat(c, b, a);
-      double X = Wabc * Vabc + Wacb * Vacb + Wbac * Vbac + Wbca * Vbca + Wcab * Vcab + Wcba * Vcba;
-      double Y = Vabc + Vbca + Vcab;
-      double Z = Vacb + Vbac + Vcba;
-      double Ef = (Y - 2 * Z) * (Wabc + Wbca + Wcab) + (Z - 2 * Y) * (Wacb + Wbac + Wcba) + 3 * X;
-      acc += Ef / ((Dab - fv[c]) * (1.0 + (a == b) + (b == c)));
+      const float Wabc = Wat(a, b, c), Wacb = Wat(a, c, b), Wbac = Wat(b, a, c);
+      const float Wbca = Wat(b, c, a), Wcab = Wat(c, a, b), Wcba = Wat(c, b, a);
+      const float Vabc = Vat(a, b, c, Wabc), Vacb = Vat(a, c, b, Wacb), Vbac = Vat(b, a, c, Wbac);
+      const float Vbca = Vat(b, c, a, Wbca), Vcab = Vat(c, a, b, Wcab), Vcba = Vat(c, b, a, Wcba);
+      const float X = Wabc * Vabc + Wacb * Vacb + Wbac * Vbac + Wbca * Vbca + Wcab * Vcab + Wcba * Vcba;
+      const float Y = Vabc + Vbca + Vcab;
+      const float Z = Vacb + Vbac + Vcba;
+      const float Ef = (Y - 2.0f * Z) * (Wabc + Wbca + Wcab) + (Z - 2.0f * Y) * (Wacb + Wbac + Wcba) + 3.0f * X;
+      const double wgt = 1.0 + (a == b) + (b == c);
+      acc += (double)Ef / ((Dab - fv[c]) * wgt);
     }
   }
   __shared__ double sm[EB / 32];
@@ -87,6 +92,11 @@ __global__ void __launch_bounds__(EB) triples_energy_batch_kernel(const float* _
     for (int w = 0; w < EB / 32; ++w) s += sm[w];
     part[(int64_t)k * gridDim.x + blockIdx.x] += (2.0 - (i == j) - (j == k)) * s;
   }
+}
+
+__global__ void to_f32_kernel(const double* __restrict__ x, float* __restrict__ y, int64_t n) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    y[t] = (float)x[t];
 }
 
 __global__ void sum_parts_kernel(const double* part, int64_t n, double* out) {
@@ -166,8 +176,14 @@ double triples_mixed(fcc_ctx* c) {
   packB(ooov.p, psr, OOrB.p);
   ooov.release();
 
-  DBuf<float> Wb;
+  DBuf<float> Wb, t1f, ovovf;
   Wb.alloc(o * v3);
+  t1f.alloc(o * v);
+  ovovf.alloc(o * v * o * v);
+  to_f32_kernel<<<152 * 4, 256, 0, s>>>(c->t1.p, t1f.p, o * v);
+  FCC_CHECK_LAUNCH();
+  to_f32_kernel<<<152 * 16, 256, 0, s>>>(c->ovov.p, ovovf.p, o * v * o * v);
+  FCC_CHECK_LAUNCH();
   DBuf<double> part, out;
   part.alloc(o * EBLOCKS);
   out.alloc(1);
@@ -213,7 +229,7 @@ double triples_mixed(fcc_ctx* c) {
       gemm_bf16x3(P3A.p, Rp3, i * v2, OOrB.p, Rp, j * o * v, Ko,
                   emap(v2, v, v, 0, v2, v, nk * v, nk, v, 0, v3, 1, -1.0, 1.0, W), err, s);
       dim3 g(EBLOCKS, (unsigned)nk);
-      triples_energy_batch_kernel<<<g, EB, 0, s>>>(W, c->t1.p, c->ovov.p, c->eps.p, (int)o, (int)v, (int)i, (int)j,
+      triples_energy_batch_kernel<<<g, EB, 0, s>>>(W, t1f.p, ovovf.p, c->eps.p, (int)o, (int)v, (int)i, (int)j,
                                                    part.p);
       FCC_CHECK_LAUNCH();
     }
