@@ -11,6 +11,7 @@
 #include <atomic>
 #include <cstring>
 #include <map>
+#include <mutex>
 
 #include "fcc_common.cuh"
 #include "fcc_tc.cuh"
@@ -490,3 +491,75 @@ void einsum1(double alpha, const char* spec, const TView& A, double beta, const 
 }
 
 }  // namespace fcc
+
+// ===================================================== allocation-free GEMM
+// fcc_gemm_f64_noalloc: the split-K FP64 (DMMA) contraction for callers that
+// must not allocate device memory -- code that runs while a CUDA graph is
+// being captured, inside a host framework that owns every device allocation
+// through its own pool, or on a latency-critical path where cudaMalloc's
+// implicit synchronisation is not acceptable.  Such callers pass their own
+// device inputs and output; the partial sums of the K slices live in the
+// fixed file-scope array below instead of a cudaMalloc'd buffer.
+//
+// The array holds FCC_NOALLOC_SCRATCH doubles (16 MiB) and stays resident on
+// every GPU that loads this library until the process exits.  Every call
+// shares it and it keeps the last call's contents: each call writes every
+// partial it later reads, so nothing needs clearing, but calls whose work
+// overlaps on the GPU (different streams, or host threads without ordering)
+// race on it and must be serialised by the caller.
+namespace {
+
+constexpr int64_t FCC_NOALLOC_SCRATCH = int64_t(1) << 21;
+__device__ __align__(256) double g_noalloc_scratch[FCC_NOALLOC_SCRATCH];
+
+// Device address of g_noalloc_scratch, looked up once per device with that
+// device current (a host-side reference to the symbol is not a device address).
+double* noalloc_scratch_ptr(int& status) {
+  static std::mutex mu;
+  static double* ptr[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { status = FCC_ERR_NO_DEVICE; return nullptr; }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) { status = FCC_ERR_CUDA; return nullptr; }
+    ptr[dev] = static_cast<double*>(p);
+  }
+  status = FCC_OK;
+  return ptr[dev];
+}
+
+}  // namespace
+
+extern "C" int fcc_gemm_f64_noalloc(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+                                    const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* stream) {
+  using namespace fcc;
+  if (M <= 0 || N <= 0 || K <= 0 || !A || !B || !C || lda < K || ldb < N || ldc < N) return FCC_ERR_BAD_ARG;
+  if (M * N > FCC_NOALLOC_SCRATCH / 2) return FCC_ERR_BAD_ARG;   // at least two K slices must fit
+  int st = FCC_OK;
+  double* scratch = noalloc_scratch_ptr(st);
+  if (!scratch) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  CtrDesc d;
+  d.M = M; d.M2 = 1; d.N = N; d.N2 = N; d.K = K; d.K2 = K; d.batch = 1;
+  d.a_m1 = lda; d.a_m2 = 0; d.a_k1 = 0; d.a_k2 = 1; d.a_b = 0;
+  d.b_k1 = 0; d.b_k2 = ldb; d.b_n1 = 0; d.b_n2 = 1; d.b_b = 0;
+  d.c_m1 = ldc; d.c_m2 = 0; d.c_n1 = 0; d.c_n2 = 1; d.c_b = 0;
+  d.alpha = alpha;
+  d.beta = beta;
+  const int64_t gm = (M + BM - 1) / BM, gn = (N + BN - 1) / BN;
+  if (gn > 65535) return FCC_ERR_BAD_ARG;
+  int64_t splits = std::min<int64_t>(std::max<int64_t>(2, (2 * 152 + gm * gn - 1) / (gm * gn)), (K + BK - 1) / BK);
+  splits = std::max<int64_t>(1, std::min<int64_t>(splits, FCC_NOALLOC_SCRATCH / (M * N)));
+  const int64_t chunk = ((K + splits - 1) / splits + BK - 1) / BK * BK;
+  splits = (K + chunk - 1) / chunk;
+  dim3 grid((unsigned)gm, (unsigned)gn, (unsigned)splits);
+  contract_f64_kernel<<<grid, NT, 0, s>>>(A, B, C, d, 0, 1, chunk, scratch);
+  if (cudaGetLastError() != cudaSuccess) return FCC_ERR_CUDA;
+  note_launch();
+  const int64_t MN = M * N;
+  splitk_reduce_kernel<<<(unsigned)std::min<int64_t>((MN + 255) / 256, 152 * 8), 256, 0, s>>>(scratch, (int)splits, C, d);
+  if (cudaGetLastError() != cudaSuccess) return FCC_ERR_CUDA;
+  note_launch();
+  return FCC_OK;
+}

@@ -26,7 +26,8 @@ FCC_PREC_MIXED = 1
 
 # every symbol include/fermicc.h declares, and the test hooks of include/fermicc_testing.h
 EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess",
-           "fcc_ccsd_run", "fcc_get_amps", "fcc_triples", "fcc_destroy", "fcc_strerror", "fcc_last_error")
+           "fcc_ccsd_run", "fcc_get_amps", "fcc_triples", "fcc_destroy", "fcc_strerror", "fcc_last_error",
+           "fcc_gemm_f64_noalloc")
 TEST_EXPORTS = ("fcc_test_contract", "fcc_stat_launches", "fcc_stream")
 
 
@@ -86,6 +87,9 @@ def load():
     lib.fcc_test_contract.restype = ctypes.c_int
     lib.fcc_stat_launches.argtypes = []
     lib.fcc_stat_launches.restype = ctypes.c_int64
+    i64 = ctypes.c_int64
+    lib.fcc_gemm_f64_noalloc.argtypes = [i64, i64, i64, ctypes.c_double, vp, i64, vp, i64, ctypes.c_double, vp, i64, vp]
+    lib.fcc_gemm_f64_noalloc.restype = ctypes.c_int
     lib.fcc_stream.argtypes = [vp]
     lib.fcc_stream.restype = ctypes.c_void_p
     for name in ("fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess", "fcc_ccsd_run",

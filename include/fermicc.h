@@ -131,6 +131,23 @@ int fcc_get_amps(fcc_ctx* ctx, double* T1, double* T2);
  * FCC_PREC_MIXED); et_out receives E(T). */
 int fcc_triples(fcc_ctx* ctx, int32_t precision, double* et_out);
 
+/* C = alpha * A.B + beta * C in FP64 on the DMMA pipe, split over K, for
+ * callers that cannot allocate device memory (while capturing a CUDA graph,
+ * inside a framework that owns all device memory through its own pool, or on
+ * a path where cudaMalloc's implicit synchronisation is not acceptable).
+ * This entry point has no counterpart in Fermi.jl.  A (M x K, leading
+ * dimension lda), B (K x N, ldb) and C (M x N, ldc) are ROW-MAJOR DEVICE
+ * arrays owned by the caller; the work is queued on `stream` (a
+ * cudaStream_t, NULL = legacy default stream) and the call returns without
+ * synchronising.  It allocates nothing: partial sums go to a fixed 16 MiB
+ * device array that every GPU loading the library keeps until exit, so
+ * M * N must not exceed 2^20 (FCC_ERR_BAD_ARG otherwise).  The first call on
+ * each device looks up that array's device address and should be made before
+ * any stream capture.  Calls share the array: calls that overlap on the GPU
+ * race and must be ordered by the caller. */
+int fcc_gemm_f64_noalloc(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+                         const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* stream);
+
 void fcc_destroy(fcc_ctx* ctx);
 const char* fcc_strerror(int code);
 /* Message of the last failing call on this context ("" if none). */
