@@ -27,7 +27,8 @@ FCC_PREC_MIXED = 1
 # every symbol include/fermicc.h declares, and the test hooks of include/fermicc_testing.h
 EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess",
            "fcc_ccsd_run", "fcc_get_amps", "fcc_triples", "fcc_destroy", "fcc_strerror", "fcc_last_error",
-           "fcc_gemm_f64_noalloc")
+           "fcc_gemm_f64_noalloc", "fcc_mlp_num_params", "fcc_mlp_create", "fcc_mlp_destroy", "fcc_mlp_get_params",
+           "fcc_mlp_set_params", "fcc_mlp_collect", "fcc_mlp_train", "fcc_mlp_grad", "fcc_mlp_guess")
 TEST_EXPORTS = ("fcc_test_contract", "fcc_stat_launches", "fcc_stream")
 
 
@@ -90,6 +91,21 @@ def load():
     i64 = ctypes.c_int64
     lib.fcc_gemm_f64_noalloc.argtypes = [i64, i64, i64, ctypes.c_double, vp, i64, vp, i64, ctypes.c_double, vp, i64, vp]
     lib.fcc_gemm_f64_noalloc.restype = ctypes.c_int
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.fcc_mlp_num_params.argtypes = []
+    lib.fcc_mlp_num_params.restype = i64
+    lib.fcc_mlp_create.argtypes = [ctypes.POINTER(vp), i32]
+    lib.fcc_mlp_destroy.argtypes = [vp]
+    lib.fcc_mlp_destroy.restype = None
+    lib.fcc_mlp_get_params.argtypes = [vp, fp, i64]
+    lib.fcc_mlp_set_params.argtypes = [vp, fp, i64]
+    lib.fcc_mlp_collect.argtypes = [vp, vp, i32]
+    lib.fcc_mlp_train.argtypes = [vp, i32, i32, ctypes.c_double, ctypes.c_uint64, dp]
+    lib.fcc_mlp_grad.argtypes = [vp, fp, fp, i32, fp, dp]
+    lib.fcc_mlp_guess.argtypes = [vp, vp]
+    for name in ("fcc_mlp_create", "fcc_mlp_get_params", "fcc_mlp_set_params", "fcc_mlp_collect", "fcc_mlp_train",
+                 "fcc_mlp_grad", "fcc_mlp_guess"):
+        getattr(lib, name).restype = ctypes.c_int
     lib.fcc_stream.argtypes = [vp]
     lib.fcc_stream.restype = ctypes.c_void_p
     for name in ("fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess", "fcc_ccsd_run",

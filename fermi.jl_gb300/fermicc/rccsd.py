@@ -95,6 +95,9 @@ class Context:
             _check(self.lib, h, rc, "fcc_upload_conv")
 
     def set_guess(self, T1, T2):
+        if T1 is None and T2 is None:   # back to the MP2 guess (built on the device)
+            _check(self.lib, self.h, self.lib.fcc_set_guess(self.h, None, None), "fcc_set_guess")
+            return
         T1f = np.asfortranarray(T1, dtype=np.float64)
         T2f = np.asfortranarray(T2, dtype=np.float64)
         _check(self.lib, self.h, self.lib.fcc_set_guess(self.h, _ptr(T1f), _ptr(T2f)), "fcc_set_guess")
@@ -170,7 +173,8 @@ class RCCSD:
     context: Context | None = field(default=None, repr=False)
 
     @classmethod
-    def compute(cls, moints, T1guess=None, T2guess=None, alg=None, context: Context | None = None) -> "RCCSD":
+    def compute(cls, moints, T1guess=None, T2guess=None, alg=None, context: Context | None = None,
+                guess_model=None) -> "RCCSD":
         alg = alg if alg is not None else get_rccsd_alg()
         if not isinstance(alg, RCCSDcuda):
             raise FermiException(f"invalid arguments for RCCSD method: {type(alg).__name__}")
@@ -182,6 +186,12 @@ class RCCSD:
             raise FermiException("give both T1guess and T2guess or neither")
         if T1guess is not None:
             ctx.set_guess(T1guess, T2guess)
+        elif Options.get("cc_gpu_guess") == "mlp":
+            from .mlp import DEFAULT_PARAMS, MLPGuess
+            model = guess_model or MLPGuess(Options.get("cc_gpu_device"), DEFAULT_PARAMS)
+            model.guess(ctx)
+        elif Options.get("cc_gpu_guess") != "mp2":
+            raise FermiException(f"cc_gpu_guess must be mp2 or mlp, got {Options.get('cc_gpu_guess')!r}")
         rc, res, lines = ctx.run(_opts_from_options())
         T1, T2 = ctx.amplitudes()
         return cls(res.guessenergy, res.correlation, res.energy, T1, T2, res.e_conv, res.t_conv,

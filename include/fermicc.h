@@ -131,6 +131,30 @@ int fcc_get_amps(fcc_ctx* ctx, double* T1, double* T2);
  * FCC_PREC_MIXED); et_out receives E(T). */
 int fcc_triples(fcc_ctx* ctx, int32_t precision, double* et_out);
 
+/* ---- learned T2 initialiser ---------------------------------------------
+ * A 16 -> 128 -> 128 -> 1 GELU MLP predicting the CCSD correction to each
+ * MP2 doubles amplitude from per-element features; BF16 weights with FP32
+ * master copies, trained by Adam on this GPU.  It only seeds the iteration
+ * (the guess argument of RCCSD(moints, T1guess, T2guess, alg), RCCSDa.jl:92);
+ * these entry points have no other counterpart in Fermi.jl. */
+typedef struct fcc_mlp fcc_mlp;
+int64_t fcc_mlp_num_params(void);
+int fcc_mlp_create(fcc_mlp** out, int32_t device);
+void fcc_mlp_destroy(fcc_mlp* m);
+/* parameters: W1[128][16] b1[128] W2[128][128] b2[128] w3[128] b3 mu[16] sd[16] (FP32) */
+int fcc_mlp_get_params(const fcc_mlp* m, float* params, int64_t n);
+int fcc_mlp_set_params(fcc_mlp* m, const float* params, int64_t n);
+/* append training samples (every stride-th element) from a converged CCSD on ctx */
+int fcc_mlp_collect(fcc_mlp* m, fcc_ctx* ctx, int32_t stride);
+/* Adam steps on the collected samples (batches drawn with `seed`); loss_log
+ * (may be NULL) receives one mean-squared error per step */
+int fcc_mlp_train(fcc_mlp* m, int32_t steps, int32_t batch, double lr, uint64_t seed, double* loss_log);
+/* gradient of the mean squared error for n host samples (n x 16 raw
+ * features, targets); grad receives the trained parameters' gradients */
+int fcc_mlp_grad(fcc_mlp* m, const float* X, const float* y, int32_t n, float* grad, double* loss);
+/* T1 = 0 and T2 = MP2 + learned correction as the starting amplitudes of ctx */
+int fcc_mlp_guess(fcc_ctx* ctx, const fcc_mlp* m);
+
 /* C = alpha * A.B + beta * C in FP64 on the DMMA pipe, split over K, for
  * callers that cannot allocate device memory (while capturing a CUDA graph,
  * inside a framework that owns all device memory through its own pool, or on

@@ -1,0 +1,77 @@
+"""Learned T2 initialiser: GPU gradients vs the CPU oracle, training, and the
+gain of the committed network over the MP2 guess."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import inputs
+from oracle import mlp as OM
+
+pytestmark = pytest.mark.gpu
+
+
+def _random_params(rng):
+    p = np.zeros(OM.NPARAM, dtype=np.float32)
+    p[OM.OFF_W1:OM.OFF_B1] = rng.standard_normal(OM.H * OM.NF) / 4
+    p[OM.OFF_B1:OM.OFF_W2] = 0.1 * rng.standard_normal(OM.H)
+    p[OM.OFF_W2:OM.OFF_B2] = rng.standard_normal(OM.H * OM.H) / 11
+    p[OM.OFF_B2:OM.OFF_W3] = 0.1 * rng.standard_normal(OM.H)
+    p[OM.OFF_W3:OM.OFF_B3] = rng.standard_normal(OM.H) / 11
+    p[OM.OFF_B3] = 0.05
+    p[OM.OFF_MU:OM.OFF_SD] = rng.standard_normal(OM.NF) * 0.1
+    p[OM.OFF_SD:] = 0.5 + rng.random(OM.NF)
+    return p
+
+
+def test_gradient_matches_cpu_oracle():
+    from fermicc.mlp import MLPGuess
+    rng = np.random.default_rng(5)
+    p = _random_params(rng)
+    m = MLPGuess(0, p)
+    X = rng.standard_normal((257, OM.NF)).astype(np.float32)
+    y = rng.standard_normal(257).astype(np.float32)
+    loss, g = m.grad(X, y)
+    lref, gref = OM.loss_and_grad(p, X.astype(np.float64), y.astype(np.float64))
+    assert abs(loss - lref) < 1e-5 * max(1.0, lref)
+    g = g[: OM.NTRAIN].astype(np.float64)
+    for lo, hi in ((OM.OFF_W1, OM.OFF_B1), (OM.OFF_B1, OM.OFF_W2), (OM.OFF_W2, OM.OFF_B2), (OM.OFF_B2, OM.OFF_W3),
+                   (OM.OFF_W3, OM.OFF_B3), (OM.OFF_B3, OM.OFF_B3 + 1)):
+        assert np.abs(g[lo:hi] - gref[lo:hi]).max() <= 2e-4 * max(1e-6, np.abs(gref[lo:hi]).max()), (lo, hi)
+
+
+def test_training_reduces_loss_and_keeps_the_fixed_point():
+    from fermicc.mlp import MLPGuess
+    from fermicc.train_guess import solve
+    m = MLPGuess(0)
+    for sd in (0, 1, 2):
+        r, ctx = solve(inputs(2, seed=sd))
+        m.collect(ctx, 2)
+        ctx.close()
+    loss = m.train(200, 4096, 1e-3, seed=3)
+    assert np.mean(loss[-20:]) < 0.7 * np.mean(loss[:5])
+    inp = inputs(2, seed=9)
+    ref, c1 = solve(inp, max_rms=1e-9, e_conv=1e-10)
+    lrn, c2 = solve(inp, guess_model=m, max_rms=1e-9, e_conv=1e-10)
+    assert ref.converged and lrn.converged
+    assert abs(ref.energy - lrn.energy) < 1e-9
+
+
+def test_committed_network_beats_the_mp2_guess():
+    # the trained parameters shipped with the package predict a T2 closer to
+    # the converged amplitudes than the MP2 guess on an unseen cluster
+    from fermicc.mlp import DEFAULT_PARAMS, MLPGuess
+    from fermicc.train_guess import solve
+    if not os.path.exists(DEFAULT_PARAMS):
+        pytest.fail("trained network missing: " + DEFAULT_PARAMS)
+    m = MLPGuess(0, DEFAULT_PARAMS)
+    inp = inputs(4, seed=777)
+    ref, ctx = solve(inp)
+    T2c = ref.T2
+    ctx.lib.fcc_set_guess(ctx.h, None, None)
+    _, T2mp2 = ctx.amplitudes()
+    m.guess(ctx)
+    _, T2mlp = ctx.amplitudes()
+    err_mp2 = np.sqrt(np.mean((T2mp2 - T2c) ** 2))
+    err_mlp = np.sqrt(np.mean((T2mlp - T2c) ** 2))
+    assert err_mlp < 0.8 * err_mp2, (err_mlp, err_mp2)
