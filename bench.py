@@ -54,11 +54,41 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--guess", default="auto", choices=["auto", "mp2", "mlp"],
+                    help="auto: the learned guess for the mixed form when its trained parameters exist")
     ap.add_argument("--waters", type=int, default=8)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-case", default=None,
+                    choices=["ccsd-fp64-iter", "ccsd-mixed-iter", "triples-mixed"],
+                    help="run one piece of the workload once (for ncu captures) and print its timing, no JSON line")
     return ap.parse_args()
+
+
+def profile_case(args, inp):
+    """One piece of the workload, for kernel profiling: one FP64 or one
+    split-BF16 CCSD iteration from the MP2 guess, or the mixed (T) on the
+    amplitudes after two mixed iterations."""
+    from fermicc import Options, RCCSD, RCCSDpT
+    from fermicc.rccsd import Context
+    Options.reset()
+    ctx = Context(inp)
+    t0 = time.perf_counter()
+    if args.profile_case.startswith("ccsd"):
+        Options.set("cc_gpu_precision", "fp64" if "fp64" in args.profile_case else "mixed")
+        Options.set("cc_max_iter", 1)
+        r = RCCSD.compute(inp, context=ctx)
+        print(json.dumps({"case": args.profile_case, "iteration_s": r.iterations[0]["seconds"]}))
+    else:
+        Options.set("cc_gpu_precision", "mixed")
+        Options.set("cc_max_iter", 2)
+        r = RCCSD.compute(inp, context=ctx)
+        Options.set("pt_gpu_precision", "mixed")
+        t0 = time.perf_counter()
+        pt = RCCSDpT.compute(r, inp)
+        print(json.dumps({"case": args.profile_case, "triples_s": time.perf_counter() - t0, "e_t": pt.correction}))
+    ctx.close()
 
 
 def dist_info():
@@ -171,6 +201,9 @@ def main():
     if args.impl == "reference":
         run_reference(args, inp)
         return
+    if args.profile_case:
+        profile_case(args, inp)
+        return
     import numpy as np
     import torch
     from fermicc import Options, RCCSD, RCCSDpT, _lib
@@ -188,12 +221,20 @@ def main():
     Options.set("cc_e_conv", E_CONV)
     Options.set("cc_max_rms", MAX_RMS)
     Options.set("cc_max_iter", 100)
+    from fermicc.mlp import DEFAULT_PARAMS, MLPGuess
+    guess = args.guess
+    if guess == "auto":
+        guess = "mlp" if (args.form == "mixed" and os.path.exists(DEFAULT_PARAMS)) else "mp2"
+    model = MLPGuess(local, DEFAULT_PARAMS) if guess == "mlp" else None
 
     ctx = Context(inp, device=local)
     stream = torch.cuda.ExternalStream(lib.fcc_stream(ctx.h))
 
     def solve():
-        ctx.lib.fcc_set_guess(ctx.h, None, None)
+        if model is not None:
+            model.guess(ctx)          # T1 = 0, T2 = MP2 + learned correction, on the device
+        else:
+            ctx.lib.fcc_set_guess(ctx.h, None, None)
         ccsd = RCCSD.compute(inp, context=ctx)
         pt = RCCSDpT.compute(ccsd, inp)
         return ccsd, pt
@@ -216,24 +257,47 @@ def main():
             times.append(e0.elapsed_time(e1) / 1e3)
             results.append((ccsd, pt))
     torch.cuda.synchronize()
-    launches = lib.fcc_stat_launches() - launches0
+    launches = (lib.fcc_stat_launches() - launches0) // max(1, args.steps)
+    # one more (untimed) step with per-launch CUDA events on the library's
+    # stream, for the per-kernel-class breakdown and the roofline
+    prof = (ctypes.c_double * 20)()
+    lib.fcc_prof_read(prof, 5)       # clear
+    lib.fcc_prof_enable(1)
+    solve()
+    torch.cuda.synchronize()
+    lib.fcc_prof_enable(0)
+    lib.fcc_prof_read(prof, 5)
     t_step = sum(times) / len(times)
-    if world > 1:
-        tt = torch.tensor([t_step], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(tt.item())
+    from fermicc.replicas import max_over_ranks
+    t_step = max_over_ranks(t_step, world, device="cuda")
     ccsd, pt = results[-1]
     it_kinds = [l["precision"] for l in ccsd.iterations]
     f_it, f_t = algorithmic_flops(inp.o, inp.v, inp.naux)
-    # dominant kernel by time: the FP64 DMMA contraction kernel of the FP64
-    # residual evaluations (the split-BF16 iterations and (T) are far shorter)
     f64_iters = [l for l in ccsd.iterations if l["precision"] == 0]
     t64 = sum(l["seconds"] for l in f64_iters) / max(1, len(f64_iters))
-    achieved = f_it / t64 / 1e12 if f64_iters else None
-    roof = {"bound": "tensor", "kernel": "contract_f64_kernel (DMMA m8n8k4) within one FP64 residual evaluation",
-            "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-            "frac": (achieved / FP64_PEAK_TFLOPS) if achieved else None, "traffic": None,
-            "peak_source": "own measurement (DMMA probe); MEASURED_PEAKS.json has no FP64 figure"}
+    # per-class kernel timing over the timed steps (CUDA events on the
+    # library's stream): launches, ms, algorithmic work, longest launch
+    cls = {0: "contract_f64_kernel (DMMA FP64)", 1: "gemm_bf16_tc_kernel (tcgen05 split-BF16)",
+           2: "pack kernels (split + gather)"}
+    peaks = {0: (FP64_PEAK_TFLOPS, "TFLOP/s"), 1: (1712.4, "TFLOP/s"), 2: (6765.7, "GB/s")}
+    kern = {}
+    for c, name in cls.items():
+        n, ms, work = prof[4 * c], prof[4 * c + 1], prof[4 * c + 2]
+        if n == 0 or ms == 0:
+            continue
+        scale = 1e9 if c != 2 else 1e6          # flop/ms -> TFLOP/s ; bytes/ms -> GB/s
+        ach = work / ms / scale
+        kern[name] = {"launches": int(n), "ms": ms, "achieved": ach, "unit": peaks[c][1],
+                      "frac": ach / peaks[c][0], "ms_per_launch": ms / n}
+    dom = max(((c, prof[4 * c + 1]) for c in cls), key=lambda x: x[1])[0]
+    n, ms, work = prof[4 * dom], prof[4 * dom + 1], prof[4 * dom + 2]
+    ach = work / ms / (1e9 if dom != 2 else 1e6) if ms else None
+    roof = {"bound": "tensor" if dom in (0, 1) else "hbm", "kernel": cls[dom], "achieved": ach,
+            "peak": peaks[dom][0], "unit": peaks[dom][1], "frac": (ach / peaks[dom][0]) if ach else None,
+            "traffic": None, "launches": int(n), "work_per_launch": (work / n) if n else None,
+            "peak_source": ("own measurement (DMMA probe; MEASURED_PEAKS.json has no FP64 figure)" if dom == 0
+                            else "MEASURED_PEAKS.json"),
+            "note": "achieved = sum of 2*M*N*K (algorithmic) over launches / sum of launch times"}
 
     e2e = None
     if not args.no_e2e and rank == 0:
@@ -256,6 +320,13 @@ def main():
         lib.fcc_default_opts(ctypes.byref(opts))
         opts.precision = 1 if args.form == "mixed" else 0
         opts.e_conv, opts.max_rms, opts.max_iter = E_CONV, MAX_RMS, 100
+        if model is not None:       # the same learned guess, through the C ABI
+            mh = ctypes.c_void_p()
+            assert lib.fcc_mlp_create(ctypes.byref(mh), local) == 0
+            pp = np.fromfile(DEFAULT_PARAMS, dtype=np.float32)
+            assert lib.fcc_mlp_set_params(mh, pp.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), pp.size) == 0
+            assert lib.fcc_mlp_guess(h, mh) == 0
+            lib.fcc_mlp_destroy(mh)
         res = _lib.FccCCSDResult()
         rc = lib.fcc_ccsd_run(h, ctypes.byref(opts), None, 0, ctypes.byref(res))
         assert rc == 0, rc
@@ -283,7 +354,8 @@ def main():
                           "parallelism": "replicas" if world > 1 else "single GPU",
                           "l2": "working set > L2 (T2 189 MB, factors 160 MB)"},
                "e_ccsd": ccsd.energy, "e_t": pt.correction, "e_total": pt.energy,
-               "iterations": len(ccsd.iterations), "iteration_kinds": it_kinds,
+               "iterations": len(ccsd.iterations), "iteration_kinds": it_kinds, "guess": guess,
+               "kernels": kern, "algorithmic_flops": {"ccsd_iteration": f_it, "triples": f_t},
                "fp64_iteration_s": t64 if f64_iters else None,
                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                "clocks": clk.summary()}

@@ -264,6 +264,86 @@ __global__ void axpby_flat_kernel(double* y, const double* x, int64_t n, double 
     y[e] = a * y[e] + b * x[e];
 }
 
+// ---- symmetric / antisymmetric particle-particle ladder
+// (Scuseria, Janssen & Schaefer, J. Chem. Phys. 89, 7382 (1988)):
+//   L_ij^ab = sum_cd t_ij^cd (ac|bd) = X+ + X-, with
+//   X+ = sum_{c<=d} t+_ij^cd W+_ab^cd,  X- = sum_{c<d} t-_ij^cd W-_ab^cd,
+//   t+- = (t^cd +- t^dc)/2 (t+^cc = t^cc),  W+- = W^cd +- W^dc (W+^cc = W^cc),
+// X+ symmetric and X- antisymmetric under (i<->j) and under (a<->b), so only
+// i <= j, a <= b (i < j, a < b for X-) are formed.
+
+// Tp[p][q] = t+ over (i<=j, c<=d), Tm[p'][q'] = t- over (i<j, c<d)
+__global__ void build_tpm_kernel(const double* __restrict__ t2, int o, int v, const int2* __restrict__ ijP,
+                                 const int2* __restrict__ ijM, const int2* __restrict__ cdP,
+                                 const int2* __restrict__ cdM, int64_t nP, int64_t nM, int64_t nij_p,
+                                 int64_t nij_m, double* __restrict__ Tp, double* __restrict__ Tm) {
+  const int64_t totP = nij_p * nP, totM = nij_m * nM;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < totP + totM; t += (int64_t)gridDim.x * blockDim.x) {
+    if (t < totP) {
+      const int64_t p = t / nP, q = t - p * nP;
+      const int2 ij = ijP[p], cd = cdP[q];
+      const double* tr = t2 + ((int64_t)ij.x * o + ij.y) * v * v;
+      Tp[t] = (cd.x == cd.y) ? tr[(int64_t)cd.x * v + cd.y]
+                             : 0.5 * (tr[(int64_t)cd.x * v + cd.y] + tr[(int64_t)cd.y * v + cd.x]);
+    } else {
+      const int64_t u = t - totP;
+      const int64_t p = u / nM, q = u - p * nM;
+      const int2 ij = ijM[p], cd = cdM[q];
+      const double* tr = t2 + ((int64_t)ij.x * o + ij.y) * v * v;
+      Tm[u] = 0.5 * (tr[(int64_t)cd.x * v + cd.y] - tr[(int64_t)cd.y * v + cd.x]);
+    }
+  }
+}
+
+// W+- rows for the pairs (a,b) of the current block from the slab
+// W[a-a0][c][b-a0][d] = (ac|bd), b in [a0, v).
+__global__ void build_wpm_kernel(const double* __restrict__ W, int v, int a0, int64_t vb, const int2* __restrict__ abP,
+                                 const int2* __restrict__ abM, int64_t rP0, int64_t nrP, int64_t rM0, int64_t nrM,
+                                 const int2* __restrict__ cdP, const int2* __restrict__ cdM, int64_t nP, int64_t nM,
+                                 double* __restrict__ Wp, double* __restrict__ Wm) {
+  const int64_t totP = nrP * nP, totM = nrM * nM;
+  auto Wat = [&](int a, int c, int b, int d) -> double {
+    return W[(((int64_t)(a - a0) * v + c) * vb + (b - a0)) * v + d];
+  };
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < totP + totM; t += (int64_t)gridDim.x * blockDim.x) {
+    if (t < totP) {
+      const int64_t r = t / nP, q = t - r * nP;
+      const int2 ab = abP[rP0 + r], cd = cdP[q];
+      Wp[t] = (cd.x == cd.y) ? Wat(ab.x, cd.x, ab.y, cd.y) : Wat(ab.x, cd.x, ab.y, cd.y) + Wat(ab.x, cd.y, ab.y, cd.x);
+    } else {
+      const int64_t u = t - totP;
+      const int64_t r = u / nM, q = u - r * nM;
+      const int2 ab = abM[rM0 + r], cd = cdM[q];
+      Wm[u] = Wat(ab.x, cd.x, ab.y, cd.y) - Wat(ab.x, cd.y, ab.y, cd.x);
+    }
+  }
+}
+
+// R2 += L for the four index orders of every (i<=j, a<=b) of the block.
+__global__ void ladder_scatter_kernel(const double* __restrict__ Xp, const double* __restrict__ Xm, int o, int v,
+                                      const int2* __restrict__ ijP, const int2* __restrict__ abP, int64_t nij_p,
+                                      int64_t rP0, int64_t nrP, int64_t rM0, int64_t nrM, double* __restrict__ R2) {
+  const int64_t tot = nij_p * nrP;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = t / nrP, r = t - p * nrP;
+    const int2 ij = ijP[p], ab = abP[rP0 + r];
+    const int i = ij.x, j = ij.y, a = ab.x, b = ab.y;
+    const double xp = Xp[p * nrP + r];
+    double xm = 0.0;
+    if (i < j && a < b) {
+      // positions in the (i<j) and (a<b) lists, both row-major
+      const int64_t pm = (int64_t)i * o - (int64_t)i * (i + 1) / 2 + (j - i - 1);
+      const int64_t rm = (int64_t)a * v - (int64_t)a * (a + 1) / 2 + (b - a - 1) - rM0;
+      xm = Xm[pm * nrM + rm];
+    }
+    const int64_t vv = (int64_t)v * v;
+    R2[((int64_t)i * o + j) * vv + (int64_t)a * v + b] += xp + xm;
+    if (a != b) R2[((int64_t)i * o + j) * vv + (int64_t)b * v + a] += xp - xm;
+    if (i != j) R2[((int64_t)j * o + i) * vv + (int64_t)a * v + b] += xp - xm;
+    if (i != j && a != b) R2[((int64_t)j * o + i) * vv + (int64_t)b * v + a] += xp + xm;
+  }
+}
+
 int grid_for(int64_t n, int threads = 256) {
   int64_t b = (n + threads - 1) / threads;
   return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 16));
@@ -330,10 +410,31 @@ void setup_integrals(fcc_ctx* c) {
   c->Foo.alloc(o * o);
   c->Bt.alloc(Q * n * n);
   c->red.alloc(RED_BLOCKS * NPART + 64);
-  // ladder: v^3 slab per virtual a, blocks of a sized to ~512 MB
+  // ladder: (ac|bd) slab for a block of virtuals a (b >= block start), blocks
+  // of a sized to ~512 MB; pair tables of the symmetric/antisymmetric channels
   int64_t per_a = v * v * v;
   c->ladder_block = std::max<int64_t>(1, std::min<int64_t>(v, (int64_t)(64ll << 20) / std::max<int64_t>(per_a, 1)));
   c->Wslab.alloc(c->ladder_block * per_a);
+  auto tri = [&](DBuf<int2>& dst, int64_t nx, bool diag) {
+    std::vector<int2> h;
+    for (int64_t x = 0; x < nx; ++x)
+      for (int64_t y = diag ? x : x + 1; y < nx; ++y) h.push_back(make_int2((int)x, (int)y));
+    dst.alloc(std::max<size_t>(h.size(), 1));
+    if (!h.empty()) FCC_CUDA(cudaMemcpy(dst.p, h.data(), sizeof(int2) * h.size(), cudaMemcpyHostToDevice));
+  };
+  tri(c->pairP_v, v, true);
+  tri(c->pairM_v, v, false);
+  tri(c->pairP_o, o, true);
+  tri(c->pairM_o, o, false);
+  const int64_t nP = v * (v + 1) / 2, nM = v * (v - 1) / 2;
+  const int64_t nijP = o * (o + 1) / 2, nijM = o * (o - 1) / 2;
+  c->Tp.alloc(nijP * nP);
+  c->Tm.alloc(std::max<int64_t>(1, nijM * nM));
+  const int64_t rows_max = c->ladder_block * v;
+  c->Wp.alloc(rows_max * nP);
+  c->Wm.alloc(std::max<int64_t>(1, rows_max * nM));
+  c->LXp.alloc(nijP * rows_max);
+  c->LXm.alloc(std::max<int64_t>(1, nijM * rows_max));
 }
 
 void make_mp2_guess(fcc_ctx* c) {
@@ -423,12 +524,35 @@ void residual(fcc_ctx* c) {
 
   // ---- doubles
   einsum(1.0, "Qai,Qbj->ijab", Btvo, Btvo, 0.0, R2, s);                 // (ai|bj)
-  // particle-particle ladder, one block of virtual a at a time (no vvvv)
-  for (int64_t a0 = 0; a0 < v; a0 += c->ladder_block) {
-    int64_t na = std::min<int64_t>(c->ladder_block, v - a0);
-    TView W = rm(c->Wslab.p, {na, v, v, v});                               // [a][c][b][d]
-    einsum(1.0, "Qac,Qbd->acbd", slice(Btvv, 1, a0, na), Btvv, 0.0, W, s);
-    einsum(1.0, "ijcd,acbd->ijab", t2, W, 1.0, slice(R2, 2, a0, na), s);
+  // particle-particle ladder in the symmetric / antisymmetric channels, one
+  // block of virtual a at a time (no vvvv is ever stored)
+  {
+    const int64_t nP = v * (v + 1) / 2, nM = v * (v - 1) / 2;
+    const int64_t nijP = o * (o + 1) / 2, nijM = o * (o - 1) / 2;
+    build_tpm_kernel<<<grid_for(nijP * nP + nijM * nM), 256, 0, s>>>(c->t2.p, (int)o, (int)v, c->pairP_o.p,
+                                                                    c->pairM_o.p, c->pairP_v.p, c->pairM_v.p, nP, nM,
+                                                                    nijP, nijM, c->Tp.p, c->Tm.p);
+    FCC_CHECK_LAUNCH();
+    auto startP = [&](int64_t a) { return a * v - a * (a - 1) / 2; };   // first (a, b>=a) row
+    auto startM = [&](int64_t a) { return a * v - a * (a + 1) / 2; };   // first (a, b>a) row
+    for (int64_t a0 = 0; a0 < v; a0 += c->ladder_block) {
+      const int64_t na = std::min<int64_t>(c->ladder_block, v - a0);
+      const int64_t vb = v - a0;
+      TView W = rm(c->Wslab.p, {na, v, vb, v});                            // [a][c][b-a0][d]
+      einsum(1.0, "Qac,Qbd->acbd", slice(Btvv, 1, a0, na), slice(Btvv, 1, a0, vb), 0.0, W, s);
+      const int64_t rP0 = startP(a0), nrP = startP(a0 + na) - rP0;
+      const int64_t rM0 = startM(a0), nrM = startM(a0 + na) - rM0;
+      build_wpm_kernel<<<grid_for(nrP * nP + nrM * nM), 256, 0, s>>>(c->Wslab.p, (int)v, (int)a0, vb, c->pairP_v.p,
+                                                                    c->pairM_v.p, rP0, nrP, rM0, nrM, c->pairP_v.p,
+                                                                    c->pairM_v.p, nP, nM, c->Wp.p, c->Wm.p);
+      FCC_CHECK_LAUNCH();
+      einsum(1.0, "pq,rq->pr", rm(c->Tp.p, {nijP, nP}), rm(c->Wp.p, {nrP, nP}), 0.0, rm(c->LXp.p, {nijP, nrP}), s);
+      if (nijM > 0 && nrM > 0)
+        einsum(1.0, "pq,rq->pr", rm(c->Tm.p, {nijM, nM}), rm(c->Wm.p, {nrM, nM}), 0.0, rm(c->LXm.p, {nijM, nrM}), s);
+      ladder_scatter_kernel<<<grid_for(nijP * nrP), 256, 0, s>>>(c->LXp.p, c->LXm.p, (int)o, (int)v, c->pairP_o.p,
+                                                                c->pairP_v.p, nijP, rP0, nrP, rM0, nrM, c->r2.p);
+      FCC_CHECK_LAUNCH();
+    }
   }
   // hole-hole ladder
   einsum(1.0, "Qki,Qlj->kilj", Btoo, Btoo, 0.0, Xo, s);

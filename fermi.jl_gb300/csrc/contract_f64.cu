@@ -246,10 +246,13 @@ void contract_f64_launch(const double* A, const double* B, double* C, const CtrD
   int64_t gm = (d.M + BM - 1) / BM, gn = (d.N + BN - 1) / BN;
   if (gn > 65535 || d.batch > 65535) fail(FCC_ERR_BAD_ARG, "contraction grid too large");
   if (d.K <= 0) fail(FCC_ERR_BAD_ARG, "empty contraction index");
+  const int pidx = prof_begin(s);
+  const double pflops = 2.0 * (double)d.M * (double)d.N * (double)d.K * (double)d.batch;
   if (d.N == 1) {
     const int64_t blocks = std::min<int64_t>((d.M + 7) / 8, 152 * 16);
     gemv_f64_kernel<<<dim3((unsigned)blocks, (unsigned)d.batch), 256, 0, s>>>(A, B, C, d);
     FCC_CHECK_LAUNCH();
+    prof_end(s, pidx, PROF_F64, pflops);
     return;
   }
   // few output tiles and a long K: split K over CTAs (partials reduced in a
@@ -269,11 +272,13 @@ void contract_f64_launch(const double* A, const double* B, double* C, const CtrD
     splitk_reduce_kernel<<<(unsigned)std::min<int64_t>((MN + 255) / 256, 152 * 8), 256, 0, s>>>(scratch.p, (int)splits,
                                                                                                  C, d);
     FCC_CHECK_LAUNCH();
+    prof_end(s, pidx, PROF_F64, pflops);
     return;
   }
   dim3 grid((unsigned)gm, (unsigned)gn, (unsigned)d.batch);
   contract_f64_kernel<<<grid, NT, 0, s>>>(A, B, C, d, d.a_m2 == 1 ? 1 : 0, d.b_n2 == 1 ? 1 : 0, d.K, nullptr);
   FCC_CHECK_LAUNCH();
+  prof_end(s, pidx, PROF_F64, pflops);
 }
 
 void tensor_axpby_launch(const TView& in, const TView& out, double alpha, double beta, cudaStream_t s) {
@@ -385,6 +390,7 @@ void run_tc(TcEngine* tc, double alpha, const TView& A, const TView& B, double b
   ep.md2 = gm[1].dim; ep.md3 = gm[2].dim; ep.ms1 = gm[0].s[2]; ep.ms2 = gm[1].s[2]; ep.ms3 = gm[2].s[2];
   ep.nd2 = gn[1].dim; ep.nd3 = gn[2].dim; ep.ns1 = gn[0].s[2]; ep.ns2 = gn[1].s[2]; ep.ns3 = gn[2].s[2];
   ep.alpha = alpha; ep.beta = beta; ep.C = C.p; ep.mode = EPI_F64;
+  ep.work = 2.0 * (double)M * (double)N * (double)K * sc.P;
   gemm_bf16x3(tc->bufA.p, M, 0, tc->bufB.p, N, 0, Kp, ep, tc->err, s);
   tc->tc_calls++;
   tc->tc_flops += 2.0 * (double)M * (double)N * (double)K * sc.P;

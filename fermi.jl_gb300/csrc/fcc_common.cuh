@@ -36,6 +36,11 @@ void note_launch();
     FCC_CUDA(cudaGetLastError());   \
   } while (0)
 
+// Opt-in kernel timing (csrc/prof.cu): classes of work.
+enum { PROF_F64 = 0, PROF_TC = 1, PROF_PACK = 2, PROF_UPDATE = 3, PROF_TRIPLES = 4, PROF_NCLS = 5 };
+int prof_begin(cudaStream_t s);
+void prof_end(cudaStream_t s, int idx, int cls, double work);
+
 // Device buffer owned by a context.
 template <class T>
 struct DBuf {

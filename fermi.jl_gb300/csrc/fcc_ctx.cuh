@@ -31,6 +31,9 @@ struct fcc_ctx {
   fcc::DBuf<double> t1, t2;   // current amplitudes [o][v], [o][o][v][v]
   fcc::DBuf<double> r1, r2;   // residuals
   fcc::DBuf<double> u, P, Cint, Dint, Xo, Wslab, Xq, Yq, Fvv, Foo;
+  // symmetric / antisymmetric pp-ladder: pair tables (int2), channels
+  fcc::DBuf<int2> pairP_v, pairM_v, pairP_o, pairM_o;   // (x<=y) and (x<y) pairs, row-major
+  fcc::DBuf<double> Tp, Tm, Wp, Wm, LXp, LXm;
   // reductions
   fcc::DBuf<double> red;      // device scratch for scalar reductions
   int64_t ladder_block = 0;

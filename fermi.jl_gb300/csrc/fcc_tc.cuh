@@ -50,6 +50,7 @@ struct EpiMap {
   int64_t piece = 0;
   int P = 3;
   uint32_t code = 0;
+  double work = 0.0;   // algorithmic BF16 flops for the timing log (0: use the padded count)
 };
 
 int64_t packed_kp(int64_t K, int P = 3);

@@ -465,8 +465,11 @@ void launch_tc(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __n
   }
   dim3 grid((unsigned)tm, (unsigned)tn, (unsigned)splits);
   if (grid.y > 65535) fail(FCC_ERR_BAD_ARG, "tensor-core grid too large");
+  const int pidx = prof_begin(s);
   gemm_bf16_tc_kernel<BN><<<grid, TC_THREADS, Cfg::SMEM, s>>>(ta, tb, a_row0, b_row0, num_k, chunk, e2, err);
   FCC_CHECK_LAUNCH();
+  // executed BF16 flops (padded K included)
+  prof_end(s, pidx, PROF_TC, ep.work > 0 ? ep.work : 2.0 * (double)ep.M * (double)ep.N * (double)Kp);
 }
 
 }  // namespace
@@ -475,6 +478,9 @@ int64_t packed_kp(int64_t K, int P) { return ((P * K + BK - 1) / BK) * BK; }
 
 void pack_split(const double* src, const PackSpec& ps, __nv_bfloat16* dst, cudaStream_t s) {
   if (ps.R <= 0 || ps.K <= 0) return;
+  const int pidx = prof_begin(s);
+  struct End { cudaStream_t s; int i; double b; ~End() { prof_end(s, i, PROF_PACK, b); } } pend{s, pidx,
+      (double)ps.R * (double)ps.K * 8.0 + (double)ps.R * (double)ps.Kp * 2.0};
   if (ps.P < 1 || ps.P > 8 || ps.Kp < ps.P * ps.K) fail(FCC_ERR_BAD_ARG, "bad pack spec");
   const int64_t kfast = std::llabs(ps.kd3 > 1 ? ps.ks3 : (ps.kd2 > 1 ? ps.ks2 : ps.ks1));
   const int64_t rfast = std::llabs(ps.rd3 > 1 ? ps.rs3 : (ps.rd2 > 1 ? ps.rs2 : ps.rs1));

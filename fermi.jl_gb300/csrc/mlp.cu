@@ -243,14 +243,36 @@ __global__ void gather_kernel(const float* X, const float* Y, int64_t B, uint64_
   }
 }
 
-// MP2 + learned correction for every element, into t2; t1 = 0.
-__global__ void infer_write_kernel(FeatSrc f, const float* y, int64_t base, int64_t n, double* t2) {
+// MP2 + lam * learned correction into t2 for the elements with
+// |t_MP2| >= thresh (the others keep their MP2 value); t1 = 0.
+__global__ void infer_write_kernel(FeatSrc f, const float* y, int64_t base, int64_t n, double lam, double thresh,
+                                   double* t2) {
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
     const int64_t e = base + s;
     float x[NF];
     double tmp2;
     features(f, e, x, tmp2);
-    t2[e] = tmp2 + (double)y[s] * (fabs(tmp2) + TARGET_FLOOR);
+    const double corr = fabs(tmp2) >= thresh ? lam * (double)y[s] * (fabs(tmp2) + TARGET_FLOOR) : 0.0;
+    t2[e] = tmp2 + corr;
+  }
+}
+
+// t_ijab = t_jiba holds for the exact amplitudes; the network sees the two
+// elements through different feature vectors, so average them.
+__global__ void pair_symmetrise_kernel(double* t2, int o, int v) {
+  const int64_t total = (int64_t)o * o * v * v;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(e % v);
+    int64_t r = e / v;
+    const int a = (int)(r % v);
+    r /= v;
+    const int j = (int)(r % o), i = (int)(r / o);
+    const int64_t e2 = (((int64_t)j * o + i) * v + b) * v + a;
+    if (e < e2) {
+      const double m = 0.5 * (t2[e] + t2[e2]);
+      t2[e] = m;
+      t2[e2] = m;
+    }
   }
 }
 
@@ -568,8 +590,9 @@ int fcc_mlp_grad(fcc_mlp* m, const float* X, const float* y, int32_t n, float* g
   });
 }
 
-// T1 = 0 and T2 = MP2 + learned correction, built on the device.
-int fcc_mlp_guess(fcc_ctx* c, const fcc_mlp* mc) {
+// T1 = 0 and T2 = MP2 + lam * learned correction (applied where
+// |t_MP2| >= thresh), built on the device.
+int fcc_mlp_guess_ex(fcc_ctx* c, const fcc_mlp* mc, double lam, double thresh) {
   fcc_mlp* m = const_cast<fcc_mlp*>(mc);
   if (!c || !m) return FCC_ERR_BAD_ARG;
   if (!c->have_ints) return FCC_ERR_STATE;
@@ -589,9 +612,11 @@ int fcc_mlp_guess(fcc_ctx* c, const fcc_mlp* mc) {
       infer_features_kernel<<<grid_of(nb), 256, 0, s>>>(f, base, nb, m->p.p + OFF_MU, m->p.p + OFF_SD, m->Xb.p);
       FCC_CHECK_LAUNCH();
       fwd_bwd(m, nb, nullptr, false);
-      infer_write_kernel<<<grid_of(nb), 256, 0, s>>>(f, m->yb.p, base, nb, c->t2.p);
+      infer_write_kernel<<<grid_of(nb), 256, 0, s>>>(f, m->yb.p, base, nb, lam, thresh, c->t2.p);
       FCC_CHECK_LAUNCH();
     }
+    pair_symmetrise_kernel<<<grid_of(total), 256, 0, s>>>(c->t2.p, (int)c->o, (int)c->v);
+    FCC_CHECK_LAUNCH();
     FCC_CUDA(cudaMemsetAsync(c->t1.p, 0, sizeof(double) * c->o * c->v, s));
     FCC_CUDA(cudaStreamSynchronize(s));
     c->have_guess = true;
@@ -599,5 +624,10 @@ int fcc_mlp_guess(fcc_ctx* c, const fcc_mlp* mc) {
     return FCC_OK;
   });
 }
+
+// Default inference settings: full correction on the amplitudes with
+// |t_MP2| >= 3e-4, MP2 elsewhere (on the many tiny amplitudes the network's
+// error is of the size of their correction).
+int fcc_mlp_guess(fcc_ctx* c, const fcc_mlp* m) { return fcc_mlp_guess_ex(c, m, 1.0, 3e-4); }
 
 }  // extern "C"

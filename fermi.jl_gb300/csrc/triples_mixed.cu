@@ -44,10 +44,10 @@ __global__ void __launch_bounds__(EB) triples_energy_batch_kernel(const float* _
                                                                   const float* __restrict__ t1f,
                                                                   const float* __restrict__ ovovf,
                                                                   const double* __restrict__ eps, int o, int v,
-                                                                  int i, int j, double* part) {
-  const int k = blockIdx.y;
+                                                                  int i, int j, int k0, double* part) {
+  const int k = k0 + blockIdx.y;
   if (i == j && j == k) return;
-  const float* W = Wb + (int64_t)k * v * v * v;
+  const float* W = Wb + (int64_t)blockIdx.y * v * v * v;
   const int64_t mstr = (int64_t)o * v;
   const float* Mjk = ovovf + ((int64_t)j * v * o + k) * v;
   const float* Mik = ovovf + ((int64_t)i * v * o + k) * v;
@@ -127,6 +127,7 @@ EpiMap emap(int64_t M, int64_t md2, int64_t md3, int64_t ms1, int64_t ms2, int64
   e.M = M; e.md2 = md2; e.md3 = md3; e.ms1 = ms1; e.ms2 = ms2; e.ms3 = ms3;
   e.N = N; e.nd2 = nd2; e.nd3 = nd3; e.ns1 = ns1; e.ns2 = ns2; e.ns3 = ns3;
   e.alpha = alpha; e.beta = beta; e.C = C; e.mode = EPI_F32;
+  e.work = 0.0;
   return e;
 }
 
@@ -177,7 +178,7 @@ double triples_mixed(fcc_ctx* c) {
   ooov.release();
 
   DBuf<float> Wb, t1f, ovovf;
-  Wb.alloc(o * v3);
+  Wb.alloc(std::max<int64_t>(1, std::min<int64_t>(o, (96ll << 20) / (v3 * 4))) * v3);
   t1f.alloc(o * v);
   ovovf.alloc(o * v * o * v);
   to_f32_kernel<<<152 * 4, 256, 0, s>>>(c->t1.p, t1f.p, o * v);
@@ -192,47 +193,53 @@ double triples_mixed(fcc_ctx* c) {
   FCC_CUDA(cudaMemsetAsync(c->dev_err.p, 0, sizeof(int), s));
   int* err = c->dev_err.p;
   const int64_t Rov = o * v2, Rp = o * o * v, Rp3 = o * v2;
+  // k is processed in chunks whose W (FP32) fits comfortably in L2, so the
+  // twelve read-modify-write epilogues and the energy pass hit L2
+  const int64_t KC = std::max<int64_t>(1, std::min<int64_t>(o, (96ll << 20) / (v3 * 4)));
   float* W = Wb.p;
   for (int64_t i = 0; i < o; ++i)
-    for (int64_t j = 0; j <= i; ++j) {
-      const int64_t nk = j + 1;
-      // W[k][a][b][c]: strides v3, v2, v, 1.  Operands are oriented so the
-      // GEMM's N index ends in c (stride 1): coalesced epilogue stores.
-      // :109  (ia|bd) t(k,j,c,d)  -  (li|jb) t(k,l,c,a)
-      gemm_bf16x3(OVpA.p, Rov, i * v2, P1.p, Rp, j * o * v, Kv,
-                  emap(v2, v, v, 0, v2, v, nk * v, nk, v, 0, v3, 1, 1.0, 0.0, W), err, s);
-      gemm_bf16x3(OOq.p, Rp, (j * o + i) * v, P3T.p, Rp3, 0, Ko,
-                  emap(v, 1, v, 0, 0, v, nk * v2, v, v, v3, v2, 1, -1.0, 1.0, W), err, s);
-      // :110  (jb|ad) t(k,i,c,d)  -  (lj|ia) t(k,l,c,b)
-      gemm_bf16x3(OVpA.p, Rov, j * v2, P1.p, Rp, i * o * v, Kv,
-                  emap(v2, v, v, 0, v, v2, nk * v, nk, v, 0, v3, 1, 1.0, 1.0, W), err, s);
-      gemm_bf16x3(OOq.p, Rp, (i * o + j) * v, P3T.p, Rp3, 0, Ko,
-                  emap(v, 1, v, 0, 0, v2, nk * v2, v, v, v3, v, 1, -1.0, 1.0, W), err, s);
-      // :111  (kc|ad) t(j,i,b,d)  -  (lk|ia) t(j,l,b,c)
-      gemm_bf16x3(P2A.p, Rp, (j * o + i) * v, OVpTB.p, Rov, 0, Kv,
-                  emap(v, 1, v, 0, 0, v, nk * v2, v, v, v3, v2, 1, 1.0, 1.0, W), err, s);
-      gemm_bf16x3(OOq.p, Rp, i * o * v, P3.p, Rp3, j * v2, Ko,
-                  emap(nk * v, nk, v, 0, v3, v2, v2, v, v, 0, v, 1, -1.0, 1.0, W), err, s);
-      // :112  (kc|bd) t(j,i,d,a)  -  (lk|jb) t(i,l,a,c)
-      gemm_bf16x3(P2A.p, Rp, (i * o + j) * v, OVpTB.p, Rov, 0, Kv,
-                  emap(v, 1, v, 0, 0, v2, nk * v2, v, v, v3, v, 1, 1.0, 1.0, W), err, s);
-      gemm_bf16x3(OOq.p, Rp, j * o * v, P3.p, Rp3, i * v2, Ko,
-                  emap(nk * v, nk, v, 0, v3, v, v2, v, v, 0, v2, 1, -1.0, 1.0, W), err, s);
-      // :113  (ia|cd) t(k,j,d,b)  -  (li|kc) t(j,l,b,a)
-      gemm_bf16x3(P2A.p, Rp, j * o * v, OVpB.p, Rov, i * v2, Kv,
-                  emap(nk * v, nk, v, 0, v3, v, v2, v, v, 0, v2, 1, 1.0, 1.0, W), err, s);
-      gemm_bf16x3(P3A.p, Rp3, j * v2, OOrB.p, Rp, i * o * v, Ko,
-                  emap(v2, v, v, 0, v, v2, nk * v, nk, v, 0, v3, 1, -1.0, 1.0, W), err, s);
-      // :114  (jb|cd) t(k,i,d,a)  -  (lj|kc) t(i,l,a,b)
-      gemm_bf16x3(P2A.p, Rp, i * o * v, OVpB.p, Rov, j * v2, Kv,
-                  emap(nk * v, nk, v, 0, v3, v2, v2, v, v, 0, v, 1, 1.0, 1.0, W), err, s);
-      gemm_bf16x3(P3A.p, Rp3, i * v2, OOrB.p, Rp, j * o * v, Ko,
-                  emap(v2, v, v, 0, v2, v, nk * v, nk, v, 0, v3, 1, -1.0, 1.0, W), err, s);
-      dim3 g(EBLOCKS, (unsigned)nk);
-      triples_energy_batch_kernel<<<g, EB, 0, s>>>(W, t1f.p, ovovf.p, c->eps.p, (int)o, (int)v, (int)i, (int)j,
-                                                   part.p);
-      FCC_CHECK_LAUNCH();
-    }
+    for (int64_t j = 0; j <= i; ++j)
+      for (int64_t k0 = 0; k0 <= j; k0 += KC) {
+        const int64_t nk = std::min<int64_t>(KC, j + 1 - k0);
+        // W[k-k0][a][b][c]: strides v3, v2, v, 1.  Operands are oriented so the
+        // GEMM's N index ends in c (stride 1): coalesced epilogue stores.
+        // :109  (ia|bd) t(k,j,c,d)  -  (li|jb) t(k,l,c,a)
+        gemm_bf16x3(OVpA.p, Rov, i * v2, P1.p, Rp, (j * o + k0) * v, Kv,
+                    emap(v2, v, v, 0, v2, v, nk * v, nk, v, 0, v3, 1, 1.0, 0.0, W), err, s);
+        gemm_bf16x3(OOq.p, Rp, (j * o + i) * v, P3T.p, Rp3, k0 * v2, Ko,
+                    emap(v, 1, v, 0, 0, v, nk * v2, v, v, v3, v2, 1, -1.0, 1.0, W), err, s);
+        // :110  (jb|ad) t(k,i,c,d)  -  (lj|ia) t(k,l,c,b)
+        gemm_bf16x3(OVpA.p, Rov, j * v2, P1.p, Rp, (i * o + k0) * v, Kv,
+                    emap(v2, v, v, 0, v, v2, nk * v, nk, v, 0, v3, 1, 1.0, 1.0, W), err, s);
+        gemm_bf16x3(OOq.p, Rp, (i * o + j) * v, P3T.p, Rp3, k0 * v2, Ko,
+                    emap(v, 1, v, 0, 0, v2, nk * v2, v, v, v3, v, 1, -1.0, 1.0, W), err, s);
+        // :111  (kc|ad) t(j,i,b,d)  -  (lk|ia) t(j,l,b,c)
+        gemm_bf16x3(P2A.p, Rp, (j * o + i) * v, OVpTB.p, Rov, k0 * v2, Kv,
+                    emap(v, 1, v, 0, 0, v, nk * v2, v, v, v3, v2, 1, 1.0, 1.0, W), err, s);
+        gemm_bf16x3(OOq.p, Rp, (i * o + k0) * v, P3.p, Rp3, j * v2, Ko,
+                    emap(nk * v, nk, v, 0, v3, v2, v2, v, v, 0, v, 1, -1.0, 1.0, W), err, s);
+        // :112  (kc|bd) t(j,i,d,a)  -  (lk|jb) t(i,l,a,c)
+        gemm_bf16x3(P2A.p, Rp, (i * o + j) * v, OVpTB.p, Rov, k0 * v2, Kv,
+                    emap(v, 1, v, 0, 0, v2, nk * v2, v, v, v3, v, 1, 1.0, 1.0, W), err, s);
+        gemm_bf16x3(OOq.p, Rp, (j * o + k0) * v, P3.p, Rp3, i * v2, Ko,
+                    emap(nk * v, nk, v, 0, v3, v, v2, v, v, 0, v2, 1, -1.0, 1.0, W), err, s);
+        // :113  (ia|cd) t(k,j,d,b)  -  (li|kc) t(j,l,b,a)
+        gemm_bf16x3(P2A.p, Rp, (j * o + k0) * v, OVpB.p, Rov, i * v2, Kv,
+                    emap(nk * v, nk, v, 0, v3, v, v2, v, v, 0, v2, 1, 1.0, 1.0, W), err, s);
+        gemm_bf16x3(P3A.p, Rp3, j * v2, OOrB.p, Rp, (i * o + k0) * v, Ko,
+                    emap(v2, v, v, 0, v, v2, nk * v, nk, v, 0, v3, 1, -1.0, 1.0, W), err, s);
+        // :114  (jb|cd) t(k,i,d,a)  -  (lj|kc) t(i,l,a,b)
+        gemm_bf16x3(P2A.p, Rp, (i * o + k0) * v, OVpB.p, Rov, j * v2, Kv,
+                    emap(nk * v, nk, v, 0, v3, v2, v2, v, v, 0, v, 1, 1.0, 1.0, W), err, s);
+        gemm_bf16x3(P3A.p, Rp3, i * v2, OOrB.p, Rp, (j * o + k0) * v, Ko,
+                    emap(v2, v, v, 0, v2, v, nk * v, nk, v, 0, v3, 1, -1.0, 1.0, W), err, s);
+        dim3 g(EBLOCKS, (unsigned)nk);
+        const int pe = prof_begin(s);
+        triples_energy_batch_kernel<<<g, EB, 0, s>>>(W, t1f.p, ovovf.p, c->eps.p, (int)o, (int)v, (int)i, (int)j,
+                                                     (int)k0, part.p);
+        FCC_CHECK_LAUNCH();
+        prof_end(s, pe, PROF_TRIPLES, (double)nk * (double)v * (v + 1) * (v + 2) / 6.0);
+      }
   sum_parts_kernel<<<1, 1, 0, s>>>(part.p, o * EBLOCKS, out.p);
   FCC_CHECK_LAUNCH();
   double et = 0.0;

@@ -28,8 +28,9 @@ FCC_PREC_MIXED = 1
 EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess",
            "fcc_ccsd_run", "fcc_get_amps", "fcc_triples", "fcc_destroy", "fcc_strerror", "fcc_last_error",
            "fcc_gemm_f64_noalloc", "fcc_mlp_num_params", "fcc_mlp_create", "fcc_mlp_destroy", "fcc_mlp_get_params",
-           "fcc_mlp_set_params", "fcc_mlp_collect", "fcc_mlp_train", "fcc_mlp_grad", "fcc_mlp_guess")
-TEST_EXPORTS = ("fcc_test_contract", "fcc_stat_launches", "fcc_stream")
+           "fcc_mlp_set_params", "fcc_mlp_collect", "fcc_mlp_train", "fcc_mlp_grad", "fcc_mlp_guess",
+           "fcc_mlp_guess_ex")
+TEST_EXPORTS = ("fcc_test_contract", "fcc_stat_launches", "fcc_stream", "fcc_prof_enable", "fcc_prof_read")
 
 
 class FccOpts(ctypes.Structure):
@@ -103,9 +104,15 @@ def load():
     lib.fcc_mlp_train.argtypes = [vp, i32, i32, ctypes.c_double, ctypes.c_uint64, dp]
     lib.fcc_mlp_grad.argtypes = [vp, fp, fp, i32, fp, dp]
     lib.fcc_mlp_guess.argtypes = [vp, vp]
+    lib.fcc_mlp_guess_ex.argtypes = [vp, vp, ctypes.c_double, ctypes.c_double]
+    lib.fcc_mlp_guess_ex.restype = ctypes.c_int
     for name in ("fcc_mlp_create", "fcc_mlp_get_params", "fcc_mlp_set_params", "fcc_mlp_collect", "fcc_mlp_train",
                  "fcc_mlp_grad", "fcc_mlp_guess"):
         getattr(lib, name).restype = ctypes.c_int
+    lib.fcc_prof_enable.argtypes = [i32]
+    lib.fcc_prof_enable.restype = ctypes.c_int
+    lib.fcc_prof_read.argtypes = [dp, i32]
+    lib.fcc_prof_read.restype = ctypes.c_int
     lib.fcc_stream.argtypes = [vp]
     lib.fcc_stream.restype = ctypes.c_void_p
     for name in ("fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess", "fcc_ccsd_run",

@@ -71,8 +71,12 @@ class MLPGuess:
         self._check(self.lib.fcc_mlp_grad(self.h, _fp(X), _fp(y), len(y), _fp(g), ctypes.byref(loss)), "fcc_mlp_grad")
         return float(loss.value), g
 
-    def guess(self, context):
-        self._check(self.lib.fcc_mlp_guess(context.h, self.h), "fcc_mlp_guess")
+    def guess(self, context, lam: float | None = None, thresh: float | None = None):
+        if lam is None and thresh is None:
+            self._check(self.lib.fcc_mlp_guess(context.h, self.h), "fcc_mlp_guess")
+        else:
+            self._check(self.lib.fcc_mlp_guess_ex(context.h, self.h, 1.0 if lam is None else lam,
+                                                  3e-4 if thresh is None else thresh), "fcc_mlp_guess_ex")
 
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:

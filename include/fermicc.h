@@ -152,8 +152,12 @@ int fcc_mlp_train(fcc_mlp* m, int32_t steps, int32_t batch, double lr, uint64_t 
 /* gradient of the mean squared error for n host samples (n x 16 raw
  * features, targets); grad receives the trained parameters' gradients */
 int fcc_mlp_grad(fcc_mlp* m, const float* X, const float* y, int32_t n, float* grad, double* loss);
-/* T1 = 0 and T2 = MP2 + learned correction as the starting amplitudes of ctx */
+/* T1 = 0 and T2 = MP2 + learned correction as the starting amplitudes of ctx
+ * (the correction is applied where |t_MP2| >= 3e-4; the result is made
+ * symmetric under (i,a) <-> (j,b)) */
 int fcc_mlp_guess(fcc_ctx* ctx, const fcc_mlp* m);
+/* same with the correction scaled by lam and applied where |t_MP2| >= thresh */
+int fcc_mlp_guess_ex(fcc_ctx* ctx, const fcc_mlp* m, double lam, double thresh);
 
 /* C = alpha * A.B + beta * C in FP64 on the DMMA pipe, split over K, for
  * callers that cannot allocate device memory (while capturing a CUDA graph,

@@ -31,6 +31,14 @@ int64_t fcc_stat_launches(void);
 typedef struct fcc_ctx fcc_ctx;
 void* fcc_stream(const fcc_ctx* ctx);
 
+/* Opt-in per-class kernel timing with CUDA events on the launching stream:
+ * classes 0 FP64 contractions (work = 2MNK flop), 1 tensor-core GEMMs (work =
+ * executed BF16 flop), 2 operand packing (work = bytes), 3 updates, 4 (T)
+ * energy.  fcc_prof_read fills out[4*c + {0,1,2,3}] = launches, total ms,
+ * work, longest launch ms for c < ncls and clears the log. */
+int fcc_prof_enable(int32_t on);
+int fcc_prof_read(double* out, int32_t ncls);
+
 #ifdef __cplusplus
 }
 #endif
