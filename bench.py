@@ -260,13 +260,13 @@ def main():
     launches = (lib.fcc_stat_launches() - launches0) // max(1, args.steps)
     # one more (untimed) step with per-launch CUDA events on the library's
     # stream, for the per-kernel-class breakdown and the roofline
-    prof = (ctypes.c_double * 20)()
-    lib.fcc_prof_read(prof, 5)       # clear
+    prof = (ctypes.c_double * 24)()
+    lib.fcc_prof_read(prof, 6)       # clear
     lib.fcc_prof_enable(1)
     solve()
     torch.cuda.synchronize()
     lib.fcc_prof_enable(0)
-    lib.fcc_prof_read(prof, 5)
+    lib.fcc_prof_read(prof, 6)
     t_step = sum(times) / len(times)
     from fermicc.replicas import max_over_ranks
     t_step = max_over_ranks(t_step, world, device="cuda")
@@ -278,8 +278,8 @@ def main():
     # per-class kernel timing over the timed steps (CUDA events on the
     # library's stream): launches, ms, algorithmic work, longest launch
     cls = {0: "contract_f64_kernel (DMMA FP64)", 1: "gemm_bf16_tc_kernel (tcgen05 split-BF16)",
-           2: "pack kernels (split + gather)"}
-    peaks = {0: (FP64_PEAK_TFLOPS, "TFLOP/s"), 1: (1712.4, "TFLOP/s"), 2: (6765.7, "GB/s")}
+           2: "pack kernels (split + gather)", 5: "gemm_oz_kernel (tcgen05 exact-slice BF16)"}
+    peaks = {0: (FP64_PEAK_TFLOPS, "TFLOP/s"), 1: (1712.4, "TFLOP/s"), 2: (6765.7, "GB/s"), 5: (1712.4, "TFLOP/s")}
     kern = {}
     for c, name in cls.items():
         n, ms, work = prof[4 * c], prof[4 * c + 1], prof[4 * c + 2]
@@ -292,7 +292,7 @@ def main():
     dom = max(((c, prof[4 * c + 1]) for c in cls), key=lambda x: x[1])[0]
     n, ms, work = prof[4 * dom], prof[4 * dom + 1], prof[4 * dom + 2]
     ach = work / ms / (1e9 if dom != 2 else 1e6) if ms else None
-    roof = {"bound": "tensor" if dom in (0, 1) else "hbm", "kernel": cls[dom], "achieved": ach,
+    roof = {"bound": "hbm" if dom == 2 else "tensor", "kernel": cls[dom], "achieved": ach,
             "peak": peaks[dom][0], "unit": peaks[dom][1], "frac": (ach / peaks[dom][0]) if ach else None,
             "traffic": None, "launches": int(n), "work_per_launch": (work / n) if n else None,
             "peak_source": ("own measurement (DMMA probe; MEASURED_PEAKS.json has no FP64 figure)" if dom == 0
