@@ -61,15 +61,15 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-case", default=None,
-                    choices=["ccsd-fp64-iter", "ccsd-mixed-iter", "triples-mixed"],
+                    choices=["ccsd-fp64-iter", "ccsd-mixed-iter", "ccsd-exact-iter", "triples-mixed"],
                     help="run one piece of the workload once (for ncu captures) and print its timing, no JSON line")
     return ap.parse_args()
 
 
 def profile_case(args, inp):
-    """One piece of the workload, for kernel profiling: one FP64 or one
-    split-BF16 CCSD iteration from the MP2 guess, or the mixed (T) on the
-    amplitudes after two mixed iterations."""
+    """One piece of the workload, for kernel profiling: one FP64, one
+    split-BF16 or one exact-slice CCSD iteration from the MP2 guess, or the
+    mixed (T) on the amplitudes after two mixed iterations."""
     from fermicc import Options, RCCSD, RCCSDpT
     from fermicc.rccsd import Context
     Options.reset()
@@ -78,8 +78,14 @@ def profile_case(args, inp):
     if args.profile_case.startswith("ccsd"):
         Options.set("cc_gpu_precision", "fp64" if "fp64" in args.profile_case else "mixed")
         Options.set("cc_max_iter", 1)
+        if "exact" in args.profile_case:
+            # one split-BF16 iteration, then (switch threshold above any rms)
+            # one exact-slice iteration
+            Options.set("cc_gpu_switch_rms", 10.0)
+            Options.set("cc_max_iter", 2)
         r = RCCSD.compute(inp, context=ctx)
-        print(json.dumps({"case": args.profile_case, "iteration_s": r.iterations[0]["seconds"]}))
+        print(json.dumps({"case": args.profile_case, "iteration_s": r.iterations[-1]["seconds"],
+                          "kinds": [l["precision"] for l in r.iterations]}))
     else:
         Options.set("cc_gpu_precision", "mixed")
         Options.set("cc_max_iter", 2)

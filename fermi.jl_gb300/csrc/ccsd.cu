@@ -768,20 +768,13 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
   int status = FCC_OK;
   bool conv_final = false;
   // Iteration kinds: FP64 residual; split-BF16 residual with three products
-  // (mixed form, first phase); six-product split-BF16 residual plus the FP64
-  // defect delta = R64(T0) - R6(T0) of the last FP64 evaluation (mixed form,
-  // finish: the six-product residual is smooth enough in T at the 1e-9 level
-  // for the correction to carry over between FP64 evaluations).  The mixed form ends
+  // (mixed form, first phase); exact-slice BF16 residual (mixed form, second
+  // phase: Ozaki-scheme products whose error, ~1e-11 absolute in the
+  // residual, is far below the convergence criteria).  The mixed form ends
   // only on an FP64 residual evaluation that meets the criteria, so its
   // converged amplitudes are the FP64 fixed point.
-  enum { K_F64 = 0, K_MIX = 1, K_CORR = 2 };
+  enum { K_F64 = 0, K_MIX = 1, K_EXACT = 2 };
   int kind = (phase == FCC_PREC_MIXED) ? K_MIX : K_F64;
-  bool finish = false;           // mixed form: in the defect-corrected finish
-  bool polish = false;           // mixed form: last plain FP64 iterations
-  int inner = 0, inner_stall = 0;
-  double inner_tol = 0.0, inner_best = 1e300;
-  DBuf<double> del1, del2;
-  auto reset_diis = [&]() { for (auto* d : {&D1s, &D2s}) std::fill(d->valid.begin(), d->valid.end(), 0); };
   while (true) {
     if (ite > op.max_iter) { status = FCC_NO_CONVERGE; break; }            // :179-182
     FCC_CUDA(cudaEventRecord(ev0, s));
@@ -790,33 +783,16 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
     if (cur2 != c->t2.p) FCC_CUDA(cudaMemcpyAsync(c->t2.p, cur2, sizeof(double) * len2, cudaMemcpyDeviceToDevice, s));
     double oldE = Ecc;
     const int iter_kind = kind;
-    if (kind == K_F64 && finish && !polish) {
-      // FP64 evaluation inside the mixed finish: R64 and delta = R64 - Rmix
-      if (!del1.p) { del1.alloc(len1); del2.alloc(len2); }
-      reset_diis();
-      { TcScope scope(nullptr); residual(c); }
-      FCC_CUDA(cudaMemcpyAsync(del1.p, c->r1.p, sizeof(double) * len1, cudaMemcpyDeviceToDevice, s));
-      FCC_CUDA(cudaMemcpyAsync(del2.p, c->r2.p, sizeof(double) * len2, cudaMemcpyDeviceToDevice, s));
-      { TcScope scope(&c->tc); c->tc.enabled = true; c->tc.scheme = SPLIT6; residual(c); }
-      axpby_flat_kernel<<<grid_for(len1), 256, 0, s>>>(del1.p, c->r1.p, len1, 1.0, -1.0);
-      FCC_CHECK_LAUNCH();
-      axpby_flat_kernel<<<grid_for(len2), 256, 0, s>>>(del2.p, c->r2.p, len2, 1.0, -1.0);
-      FCC_CHECK_LAUNCH();
-      axpby_flat_kernel<<<grid_for(len1), 256, 0, s>>>(c->r1.p, del1.p, len1, 1.0, 1.0);
-      FCC_CHECK_LAUNCH();
-      axpby_flat_kernel<<<grid_for(len2), 256, 0, s>>>(c->r2.p, del2.p, len2, 1.0, 1.0);
-      FCC_CHECK_LAUNCH();
-    } else {
+    {
       TcScope scope(kind == K_F64 ? nullptr : &c->tc);
       c->tc.enabled = kind != K_F64;
-      c->tc.scheme = kind == K_CORR ? SPLIT6 : SPLIT3;
+      c->tc.exact = kind == K_EXACT;
+      // exact-slice width: 6 weight groups (15 slice pairs, ~3e-9 of the
+      // largest terms) while the amplitudes still move by more than max_rms,
+      // 8 groups (28 pairs, ~1e-12) for the last iterations
+      c->tc.oz_groups = rms >= op.max_rms ? 6 : OZ_G_DEFAULT;
+      c->tc.scheme = SPLIT3;
       residual(c);                                                         // :190
-      if (kind == K_CORR) {
-        axpby_flat_kernel<<<grid_for(len1), 256, 0, s>>>(c->r1.p, del1.p, len1, 1.0, 1.0);
-        FCC_CHECK_LAUNCH();
-        axpby_flat_kernel<<<grid_for(len2), 256, 0, s>>>(c->r2.p, del2.p, len2, 1.0, 1.0);
-        FCC_CHECK_LAUNCH();
-      }
     }
     double ss1, ss2, e_dummy, e_new;
     run_update(2, D1s, c->dvec1, c->derr1s, c->derr1d, c->t1.p, c->r1.p, tn1, &cur1, nullptr, &ss1, &e_dummy);
@@ -846,33 +822,27 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
     }
     Ecc = e_new;                                                           // :218
     rms = std::max(r1, r2);                                                // :220
+    const double prev_dE = dE;
     dE = Ecc - oldE;                                                       // :221
     bool converged = iter_kind == K_F64 && std::fabs(dE) < op.e_conv && rms < op.max_rms;   // :178
     if (phase == FCC_PREC_MIXED && !converged) {
-      if (iter_kind == K_MIX) {
-        // leave the split-BF16 phase once the residual is below the threshold,
-        // or when it stops improving (its noise floor)
-        if (rms < best_rms * 0.7) { best_rms = std::min(best_rms, rms); stalled = 0; }
-        else ++stalled;
-        if (rms < op.mixed_switch_rms || stalled >= 3) { finish = true; kind = K_F64; }
-      } else if (iter_kind == K_F64 && !polish) {
-        if (rms < 30.0 * op.max_rms) {
-          // near the six-product noise floor (~1e-9..1e-8): finish with plain
-          // FP64 Jacobi/DIIS iterations
-          polish = true;
-          reset_diis();
-        } else {
-          kind = K_CORR;
-          inner = 0;
-          inner_stall = 0;
-          inner_best = 1e300;
-          inner_tol = std::max(1e-3 * rms, 0.1 * op.max_rms);
-        }
-      } else if (iter_kind == K_CORR) {
-        ++inner;
-        if (rms < 0.8 * inner_best) { inner_best = rms; inner_stall = 0; }
-        else ++inner_stall;
-        if (rms < inner_tol || inner_stall >= 2 || inner >= 12) kind = K_F64;
+      // leave a reduced-precision phase once its residual is below the
+      // threshold (split-BF16: mixed_switch_rms; exact-slice: the reference's
+      // own criteria, checked next by an FP64 evaluation), or when it stops
+      // improving (its noise floor)
+      if (rms < best_rms * 0.7) { best_rms = rms; stalled = 0; }
+      else ++stalled;
+      if (iter_kind == K_MIX && (rms < op.mixed_switch_rms || stalled >= 3)) {
+        kind = K_EXACT;
+        best_rms = 1e300;
+        stalled = 0;
+      } else if (iter_kind == K_EXACT) {
+        // ten times inside the criteria on this iteration and inside them on
+        // the previous one, so that the FP64 step that follows (whose energy
+        // change is the next step of the same convergence) meets them at once
+        const bool tight = rms < 0.1 * op.max_rms && std::fabs(dE) < 0.1 * op.e_conv &&
+                           std::fabs(prev_dE) < op.e_conv;
+        if (tight || stalled >= 3) kind = K_F64;
       }
     }
     FCC_CUDA(cudaEventRecord(ev1, s));
@@ -880,7 +850,7 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
     float ms = 0;
     FCC_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
     if (!std::isfinite(Ecc) || !std::isfinite(rms)) { status = FCC_ERR_NAN; }
-    if (iter_kind != K_F64 || (finish && !polish)) {
+    if (iter_kind != K_F64) {
       int herr = 0;
       FCC_CUDA(cudaMemcpy(&herr, c->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost));
       if (herr) { status = FCC_ERR_TIMEOUT; }

@@ -375,6 +375,32 @@ void run_tc(TcEngine* tc, double alpha, const TView& A, const TView& B, double b
   order(gk, 0);
   pad3(gm); pad3(gn); pad3(gk);
   const int64_t M = gdim(gm), N = gdim(gn), K = gdim(gk);
+  if (tc->exact) {
+    // exact-slice products: S digit slices of each operand, FP64 output
+    const int G = tc->oz_groups, S = G - 1;
+    const int64_t Kpad = oz_kpad(K), W = S * Kpad;
+    if ((int64_t)tc->bufA.n < M * W) tc->bufA.alloc(M * W);
+    if ((int64_t)tc->bufB.n < N * W) tc->bufB.alloc(N * W);
+    if ((int64_t)tc->exA.n < M) tc->exA.alloc(M);
+    if ((int64_t)tc->exB.n < N) tc->exB.alloc(N);
+    PackSpec pa{M, K, W, gm[1].dim, gm[2].dim, gm[0].s[0], gm[1].s[0], gm[2].s[0],
+                gk[1].dim, gk[2].dim, gk[0].s[0], gk[1].s[0], gk[2].s[0], S, 0};
+    PackSpec pb{N, K, W, gn[1].dim, gn[2].dim, gn[0].s[1], gn[1].s[1], gn[2].s[1],
+                gk[1].dim, gk[2].dim, gk[0].s[1], gk[1].s[1], gk[2].s[1], S, 0};
+    pack_oz(A.p, pa, S, tc->bufA.p, tc->exA.p, s);
+    pack_oz(B.p, pb, S, tc->bufB.p, tc->exB.p, s);
+    EpiMap ep;
+    ep.M = M; ep.N = N;
+    ep.md2 = gm[1].dim; ep.md3 = gm[2].dim; ep.ms1 = gm[0].s[2]; ep.ms2 = gm[1].s[2]; ep.ms3 = gm[2].s[2];
+    ep.nd2 = gn[1].dim; ep.nd3 = gn[2].dim; ep.ns1 = gn[0].s[2]; ep.ns2 = gn[1].s[2]; ep.ns3 = gn[2].s[2];
+    ep.alpha = alpha; ep.beta = beta; ep.C = C.p; ep.mode = EPI_F64;
+    const double npairs = (double)(G - 1) * (double)G / 2.0;
+    ep.work = 2.0 * (double)M * (double)N * (double)K * npairs;
+    gemm_oz(tc->bufA.p, M, tc->exA.p, tc->bufB.p, N, tc->exB.p, Kpad, G, ep, tc->err, s);
+    tc->tc_calls++;
+    tc->tc_flops += ep.work;
+    return;
+  }
   const SplitScheme sc = tc->scheme;
   const int64_t Kp = packed_kp(K, sc.P);
   if ((int64_t)tc->bufA.n < M * Kp) tc->bufA.alloc(M * Kp);

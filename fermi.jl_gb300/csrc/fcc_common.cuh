@@ -37,7 +37,7 @@ void note_launch();
   } while (0)
 
 // Opt-in kernel timing (csrc/prof.cu): classes of work.
-enum { PROF_F64 = 0, PROF_TC = 1, PROF_PACK = 2, PROF_UPDATE = 3, PROF_TRIPLES = 4, PROF_NCLS = 5 };
+enum { PROF_F64 = 0, PROF_TC = 1, PROF_PACK = 2, PROF_UPDATE = 3, PROF_TRIPLES = 4, PROF_OZ = 5, PROF_NCLS = 6 };
 int prof_begin(cudaStream_t s);
 void prof_end(cudaStream_t s, int idx, int cls, double work);
 

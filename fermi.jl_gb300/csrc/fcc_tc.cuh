@@ -1,5 +1,6 @@
 // Split-BF16 tensor-core contraction: operand packing and the tcgen05 GEMM.
 #pragma once
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include "fcc_common.cuh"
@@ -30,6 +31,7 @@ struct PackSpec {
   int64_t kd2, kd3, ks1, ks2, ks3;
   int P = 3;
   uint32_t code = 0;
+  double scale = 1.0;   // the source is multiplied by this (exact for +-1 and powers of two)
 };
 
 // Output scatter of the GEMM: element (m, n) goes to
@@ -60,12 +62,41 @@ void pack_split(const double* src, const PackSpec& ps, __nv_bfloat16* dst, cudaS
 void gemm_bf16x3(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __nv_bfloat16* B, int64_t b_rows,
                  int64_t b_row0, int64_t Kp, const EpiMap& ep, int* err, cudaStream_t s);
 
+// 2-D TMA map over a row-major [rows][cols] BF16 array, boxes of 64 columns
+// (one 128-byte swizzle atom) x box_rows rows; cols must be a multiple of 64.
+CUtensorMap tma_map_bf16(const __nv_bfloat16* base, int64_t rows, int64_t cols, int box_rows);
+// C = beta * C over an epilogue map (before a GEMM adds into C atomically)
+void scale_output(const EpiMap& ep, double beta, cudaStream_t s);
+
+// Exact-slice products (the Ozaki scheme: Ozaki, Ogita, Oishi & Rump, Numer.
+// Algorithms 59, 95 (2012); on tensor cores: Mukunoki et al., ISC 2020).
+// Each row r of an operand is scaled by 2^e_r (|x| < 2^e_r over the row) and
+// cut into S = G-1 signed 6-bit digit slices, x = 2^e_r sum_s d_s 2^(-6(s+1)),
+// |d| <= 64, stored exactly in BF16.  A.B^T is the sum over slice pairs
+// (s, t) with s + t + 2 <= G of the digit products; pairs of one weight
+// 2^(-6(s+t+2)) are summed on the tensor cores in FP32 over chunks of 1024
+// products (|sum| < 2^22, so every partial sum is an exact integer) and the
+// chunks are added in double-FP32 (~2^-48 relative) in TMEM.  The result
+// carries the slice truncation error, ~2^(-6(G-1)) of max|A_r| max|B_c| per
+// term (G = 8: ~1e-12 of max|C| for Gaussian operands).
+constexpr int OZ_G_DEFAULT = 8;
+// packed layout: row r holds slice s at columns [s*Kpad, s*Kpad + K), zero up
+// to (s+1)*Kpad; ex[r] = biased FP64 exponent of max_k |x_rk| (0: all zero)
+int64_t oz_kpad(int64_t K);
+void pack_oz(const double* src, const PackSpec& ps, int S, __nv_bfloat16* dst, int* ex, cudaStream_t s);
+// FP64 epilogue (EPI_F64) of the exact-slice product over packed operands
+void gemm_oz(const __nv_bfloat16* A, int64_t a_rows, const int* exA, const __nv_bfloat16* B, int64_t b_rows,
+             const int* exB, int64_t Kpad, int G, const EpiMap& ep, int* err, cudaStream_t s);
+
 // Engine state for einsum calls that run on the tensor cores: scratch for
 // the packed operands, the device error flag, the routing threshold and
 // counters of what ran.
 struct TcEngine {
   bool enabled = false;
   SplitScheme scheme = SPLIT3;
+  bool exact = false;      // exact-slice products instead of the split scheme
+  int oz_groups = OZ_G_DEFAULT;
+  DBuf<int> exA, exB;
   double min_flops = 1e6;
   int64_t min_dim = 16;   // smallest M and N routed to the tensor cores
   DBuf<__nv_bfloat16> bufA, bufB;

@@ -56,6 +56,12 @@ extern "C" int fcc_test_contract(int32_t precision, const char* spec, const doub
     fcc::TcEngine eng;
     eng.enabled = precision != FCC_PREC_FP64;
     if (precision == 2) eng.scheme = fcc::SPLIT6;
+    if (precision == 3 || (precision >= 12 && precision <= 18)) {
+      eng.exact = true;
+      eng.oz_groups = precision == 3 ? fcc::OZ_G_DEFAULT : precision - 10;
+    } else if (precision < 0 || precision > 3) {
+      return FCC_ERR_BAD_ARG;
+    }
     eng.min_flops = 0.0;
     eng.min_dim = 1;
     eng.err = err.p;

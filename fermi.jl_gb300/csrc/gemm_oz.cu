@@ -1,0 +1,571 @@
+// Exact-slice BF16 tensor-core contraction (the Ozaki scheme) for GB300.
+//
+// C = alpha * A.B^T + beta * C for FP64 operands, evaluated from signed 6-bit
+// digit slices of A and B (see fcc_tc.cuh).  Every digit is an integer
+// |d| <= 64, exact in BF16; every product of two digits is an integer of at
+// most 2^12, so a run of 1024 products accumulated by tcgen05.mma in FP32
+// stays an exact integer (< 2^22).  The kernel therefore closes an
+// accumulation chunk every 16 k-blocks (or at the end of a weight group), and
+// the epilogue warps add the chunk, times its weight 2^(-6g) (exact), into a
+// double-FP32 (hi + lo, ~2^-48 relative) running sum held in TMEM.  Two TMEM
+// accumulators alternate, so the MMA thread fills one while the epilogue
+// drains the other.  The final epilogue converts hi and lo to FP64 with the
+// row and column scales applied by integer exponent arithmetic (the FP64 pipe
+// is 1/64 rate) and stores or reduces (red.add) into C.
+//
+// TMEM columns (128 x 512 x 32-bit): [0,128) and [128,256) chunk
+// accumulators, [256,384) hi and [384,512) lo words of the running sums.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+#include "fcc_tc.cuh"
+#include "fcc_tcgen05.cuh"
+
+namespace fcc {
+
+namespace {
+
+using namespace tc5;
+
+constexpr int OZ_BM = 128;
+constexpr int OZ_BN = 128;
+constexpr int OZ_BK = 64;
+constexpr int OZ_STAGES = 5;
+constexpr int OZ_THREADS = 192;      // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int OZ_BITS = 6;           // bits per digit slice
+constexpr int OZ_CH = 16;            // k-blocks per exact FP32 chunk (16 * 64 = 1024 products)
+constexpr int OZ_MAXPAIRS = 40;
+constexpr int OZ_A_BYTES = OZ_BM * OZ_BK * 2;
+constexpr int OZ_B_BYTES = OZ_BN * OZ_BK * 2;
+constexpr int OZ_STAGE_BYTES = OZ_A_BYTES + OZ_B_BYTES;
+constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE_BYTES + 1024;
+constexpr int OZ_COL_LO = 256, OZ_COL_HI = 384;
+
+// Slice pairs in the order of the k loop: by weight group g = sa + sb + 2,
+// then by sa; next[p] = first pair of the following group.
+struct OzPairs {
+  int n;
+  int8_t sa[OZ_MAXPAIRS], sb[OZ_MAXPAIRS], g[OZ_MAXPAIRS];
+  int16_t next[OZ_MAXPAIRS];
+};
+
+OzPairs make_pairs(int G) {
+  OzPairs p;
+  std::memset(&p, 0, sizeof(p));
+  const int S = G - 1;
+  for (int g = 2; g <= G; ++g) {
+    const int first = p.n;
+    for (int a = 1; a < g; ++a) {
+      const int b = g - a;
+      if (a > S || b > S) continue;
+      p.sa[p.n] = (int8_t)(a - 1);
+      p.sb[p.n] = (int8_t)(b - 1);
+      p.g[p.n] = (int8_t)g;
+      ++p.n;
+    }
+    for (int q = first; q < p.n; ++q) p.next[q] = (int16_t)p.n;
+  }
+  return p;
+}
+
+// end of the chunk that starts at step st: at most OZ_CH steps, never across
+// a weight group or the end of this CTA's step range
+__device__ __forceinline__ int oz_chunk_end(const OzPairs& pr, int nkb, int st, int st1) {
+  const int gend = (int)pr.next[st / nkb] * nkb;
+  return min(min(st + OZ_CH, gend), st1);
+}
+
+// 2^e as a double (0 below the normal range)
+__device__ __forceinline__ double oz_pow2(int e) {
+  if (e < -1022) return 0.0;
+  if (e > 1023) e = 1023;
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+// frexp-style exponent of the row scale from the stored biased exponent
+__device__ __forceinline__ int oz_row_exp(int be) { return be ? be - 1022 : 0; }
+
+// hi + lo += v in double-FP32 (TwoSum, then renormalisation)
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float v) {
+  const float s = __fadd_rn(hi, v);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v, bb));
+  const float l = __fadd_rn(lo, err);
+  const float h = __fadd_rn(s, l);
+  lo = __fsub_rn(l, __fsub_rn(h, s));
+  hi = h;
+}
+
+// (double)f * 2^e (negated if neg) by integer exponent arithmetic; FP32
+// subnormals and results below the FP64 normal range give 0
+__device__ __forceinline__ double f32_to_f64_scaled(float f, int e, bool neg) {
+  const uint32_t b = __float_as_uint(f);
+  const int ex = (int)((b >> 23) & 0xFF);
+  if (ex == 0) return 0.0;
+  int ne = ex - 127 + 1023 + e;
+  if (ne <= 0) return 0.0;
+  if (ne > 2046) ne = 2047;
+  const unsigned long long sign = (unsigned long long)((b >> 31) ^ (neg ? 1u : 0u)) << 63;
+  const unsigned long long bits = sign | ((unsigned long long)ne << 52) | ((unsigned long long)(b & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]),
+      "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]),
+      "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    gemm_oz_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int nkb,
+                   int kpad, const __grid_constant__ OzPairs pr, int steps_per_split, const int* __restrict__ exA,
+                   const int* __restrict__ exB, int G, EpiMap ep, int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[OZ_STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[OZ_STAGES];
+  __shared__ __align__(8) uint64_t accf_bar[2];   // chunk accumulator b is complete
+  __shared__ __align__(8) uint64_t acce_bar[2];   // chunk accumulator b is drained
+  __shared__ __align__(8) uint64_t done_bar;      // every issued MMA has completed
+  __shared__ uint32_t tmem_holder;
+  __shared__ int abort_flag;
+  __shared__ double otile[4][32][33];             // per epilogue warp: 32 x 32 transpose
+
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + OZ_STAGES * OZ_A_BYTES;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < OZ_STAGES; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), 1);
+      mbar_init(smem_u32(&empty_bar[s]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&accf_bar[b]), 1);
+      mbar_init(smem_u32(&acce_bar[b]), 4);   // one arrival per epilogue warp
+    }
+    mbar_init(smem_u32(&done_bar), 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_holder)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_holder;
+  const int64_t m0 = (int64_t)blockIdx.x * OZ_BM;
+  const int64_t n0 = (int64_t)blockIdx.y * OZ_BN;
+  const int total = pr.n * nkb;
+  const int st0 = (int)blockIdx.z * steps_per_split;
+  const int st1 = min(total, st0 + steps_per_split);
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer
+    int it = 0;
+    for (int st = st0; st < st1; ++st, ++it) {
+      const int s = it % OZ_STAGES;
+      const uint32_t ph = (it / OZ_STAGES) & 1;
+      if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1)) { atomicExch(&abort_flag, 1); break; }
+      if (*(volatile int*)&abort_flag) break;
+      const int p = st / nkb, kb = st - p * nkb;
+      const uint32_t fb = smem_u32(&full_bar[s]);
+      mbar_expect_tx(fb, OZ_STAGE_BYTES);
+      tma_load_2d(smem_u32(sA + s * OZ_A_BYTES), &tmA, (int)pr.sa[p] * kpad + kb * OZ_BK, (int32_t)m0, fb);
+      tma_load_2d(smem_u32(sB + s * OZ_B_BYTES), &tmB, (int)pr.sb[p] * kpad + kb * OZ_BK, (int32_t)n0, fb);
+    }
+    // on an abort, wait (bounded) for the loads still in flight before the
+    // shared memory can be released
+    if (*(volatile int*)&abort_flag) {
+      for (int j = max(0, it - OZ_STAGES); j < it; ++j)
+        (void)mbar_wait(smem_u32(&full_bar[j % OZ_STAGES]), (j / OZ_STAGES) & 1);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    constexpr uint32_t idesc = idesc_bf16(OZ_BM, OZ_BN);
+    int it = 0, chunk = 0;
+    bool ok = true;
+    for (int st = st0; st < st1 && ok;) {
+      const int ce = oz_chunk_end(pr, nkb, st, st1);
+      const int b = chunk & 1;
+      if (!mbar_wait(smem_u32(&acce_bar[b]), ((chunk >> 1) & 1) ^ 1)) { atomicExch(&abort_flag, 1); break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t dcol = tmem + (uint32_t)(b * OZ_BN);
+      for (int x = st; x < ce; ++x, ++it) {
+        const int s = it % OZ_STAGES;
+        const uint32_t ph = (it / OZ_STAGES) & 1;
+        if (!mbar_wait(smem_u32(&full_bar[s]), ph)) { atomicExch(&abort_flag, 1); ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint64_t ad = sw128_desc(smem_u32(sA + s * OZ_A_BYTES));
+        const uint64_t bd = sw128_desc(smem_u32(sB + s * OZ_B_BYTES));
+#pragma unroll
+        for (int kk = 0; kk < OZ_BK / 16; ++kk) {
+          const uint32_t acc = (x > st || kk > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dcol),
+              "l"(ad + (uint64_t)(2 * kk)), "l"(bd + (uint64_t)(2 * kk)), "r"(idesc), "r"(acc)
+              : "memory");
+        }
+        tc_commit(smem_u32(&empty_bar[s]));
+      }
+      if (!ok) break;
+      tc_commit(smem_u32(&accf_bar[b]));
+      st = ce;
+      ++chunk;
+    }
+    tc_commit(smem_u32(&done_bar));
+  } else if (warp >= 2) {
+    // ---------------- epilogue warps: rows q*32 .. q*32+31 of the tile
+    const int q = warp & 3;
+    const uint32_t lanebase = tmem + ((uint32_t)(q * 32) << 16);
+    bool ok = true;
+    int chunk = 0;
+    for (int st = st0; st < st1;) {
+      const int ce = oz_chunk_end(pr, nkb, st, st1);
+      const int g = pr.g[st / nkb];
+      const int b = chunk & 1;
+      ok = mbar_wait(smem_u32(&accf_bar[b]), (chunk >> 1) & 1);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok || __any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0)) { atomicExch(&abort_flag, 1); ok = false; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // weight of the group, 2^(-6g), exact in FP32
+      const float wg = __int_as_float((127 - OZ_BITS * g) << 23);
+#pragma unroll 1
+      for (int c0 = 0; c0 < OZ_BN; c0 += 32) {
+        uint32_t acc[32], hi[32], lo[32];
+        tmem_ld32(lanebase + (uint32_t)(b * OZ_BN + c0), acc);
+        if (chunk > 0) {
+          tmem_ld32(lanebase + (uint32_t)(OZ_COL_HI + c0), hi);
+          tmem_ld32(lanebase + (uint32_t)(OZ_COL_LO + c0), lo);
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int jj = 0; jj < 32; ++jj) {
+          // the chunk sum is an exact integer below 2^22; times 2^(-6g) exact
+          const float v = __fmul_rn(__uint_as_float(acc[jj]), wg);
+          float h = chunk > 0 ? __uint_as_float(hi[jj]) : 0.0f;
+          float l = chunk > 0 ? __uint_as_float(lo[jj]) : 0.0f;
+          ff_add(h, l, v);
+          hi[jj] = __float_as_uint(h);
+          lo[jj] = __float_as_uint(l);
+        }
+        tmem_st32(lanebase + (uint32_t)(OZ_COL_HI + c0), hi);
+        tmem_st32(lanebase + (uint32_t)(OZ_COL_LO + c0), lo);
+      }
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&acce_bar[b]));
+      st = ce;
+      ++chunk;
+    }
+    // every MMA is complete before TMEM is read for the last time or freed
+    bool dn = mbar_wait(smem_u32(&done_bar), 0);
+    dn = __all_sync(0xffffffffu, dn);
+    if (!dn) atomicExch(&abort_flag, 1);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool abort_now = __any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0);
+    if (ok && dn && !abort_now && chunk > 0) {
+      const int row = q * 32 + lane;
+      const int64_t m = m0 + row;
+      int64_t crow = 0;
+      int erow = 0;
+      if (m < ep.M) {
+        int64_t m3 = m % ep.md3, r = m / ep.md3;
+        int64_t m2 = r % ep.md2, m1 = r / ep.md2;
+        crow = m1 * ep.ms1 + m2 * ep.ms2 + m3 * ep.ms3;
+        erow = oz_row_exp(exA[m]);
+      }
+      // alpha = +-2^ka folds into the exponent arithmetic; otherwise one FP64 multiply
+      const unsigned long long ab = (unsigned long long)__double_as_longlong(ep.alpha);
+      const bool apow2 = (ab & ((1ull << 52) - 1)) == 0 && ((ab >> 52) & 0x7FF) != 0;
+      const int ka = apow2 ? (int)((ab >> 52) & 0x7FF) - 1023 : 0;
+      const bool aneg = apow2 && (ab >> 63);
+      double (*tile)[33] = otile[q];
+#pragma unroll 1
+      for (int c0 = 0; c0 < OZ_BN; c0 += 32) {
+        if (n0 + c0 >= ep.N) break;
+        uint32_t hi[32], lo[32];
+        tmem_ld32(lanebase + (uint32_t)(OZ_COL_HI + c0), hi);
+        tmem_ld32(lanebase + (uint32_t)(OZ_COL_LO + c0), lo);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        // this lane's column exponent, broadcast per column below
+        const int64_t nl = n0 + c0 + lane;
+        const int ecl = nl < ep.N ? oz_row_exp(exB[nl]) : 0;
+        __syncwarp();
+#pragma unroll
+        for (int jj = 0; jj < 32; ++jj) {
+          const int e = erow + __shfl_sync(0xffffffffu, ecl, jj) + ka;
+          tile[lane][jj] = f32_to_f64_scaled(__uint_as_float(hi[jj]), e, aneg) +
+                           f32_to_f64_scaled(__uint_as_float(lo[jj]), e, aneg);
+        }
+        __syncwarp();
+        const int64_t n = n0 + c0 + lane;
+        const bool nok = n < ep.N;
+        int64_t coff = 0;
+        if (nok) {
+          int64_t n3 = n % ep.nd3, rr = n / ep.nd3;
+          int64_t n2 = rr % ep.nd2, n1 = rr / ep.nd2;
+          coff = n1 * ep.ns1 + n2 * ep.ns2 + n3 * ep.ns3;
+        }
+#pragma unroll
+        for (int jr = 0; jr < 32; ++jr) {
+          const int64_t roff = __shfl_sync(0xffffffffu, crow, jr);
+          const int64_t mm = m0 + q * 32 + jr;
+          if (mm >= ep.M || !nok) continue;
+          double val = tile[jr][lane];
+          if (!apow2) val *= ep.alpha;
+          double* dst = static_cast<double*>(ep.C) + roff + coff;
+          if (ep.atomic) atomicAdd(dst, val);
+          else *dst = val;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+  }
+  if (threadIdx.x == 0 && abort_flag) atomicExch(err, 1);
+}
+
+// ---------------------------------------------------------------- packing
+
+__device__ __forceinline__ int64_t oz_row_off(const PackSpec& ps, int64_t r) {
+  const int64_t r3 = r % ps.rd3, q = r / ps.rd3;
+  return (q / ps.rd2) * ps.rs1 + (q % ps.rd2) * ps.rs2 + r3 * ps.rs3;
+}
+__device__ __forceinline__ int64_t oz_col_off(const PackSpec& ps, int64_t k) {
+  const int64_t k3 = k % ps.kd3, q = k / ps.kd3;
+  return (q / ps.kd2) * ps.ks1 + (q % ps.kd2) * ps.ks2 + k3 * ps.ks3;
+}
+__device__ __forceinline__ int biased_exp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7FF); }
+
+// ex[r] = max over the row of the biased exponent (ex zeroed before), for
+// sources whose k index is the faster one: a warp per (row, k-slab)
+__global__ void oz_exp_rows_kernel(const double* __restrict__ src, PackSpec ps, int64_t kslab, int* __restrict__ ex) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nks = (ps.K + kslab - 1) / kslab;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < ps.R * nks; w += nw) {
+    const int64_t r = w / nks, k0 = (w % nks) * kslab, k1 = min(ps.K, k0 + kslab);
+    const int64_t ro = oz_row_off(ps, r);
+    int m = 0;
+    for (int64_t k = k0 + lane; k < k1; k += 32) m = max(m, biased_exp(src[ro + oz_col_off(ps, k)]));
+    m = __reduce_max_sync(0xffffffffu, m);
+    if (lane == 0 && m > 0) atomicMax(ex + r, m);
+  }
+}
+
+// same for sources whose row index is the faster one: 32 rows x 8 k-lanes
+// per block over one k-slab
+__global__ void oz_exp_tiles_kernel(const double* __restrict__ src, PackSpec ps, int64_t kslab, int* __restrict__ ex) {
+  __shared__ int red[8][32];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int64_t nrt = (ps.R + 31) / 32, nks = (ps.K + kslab - 1) / kslab;
+  for (int64_t tb = blockIdx.x; tb < nrt * nks; tb += gridDim.x) {
+    const int64_t r = (tb / nks) * 32 + tx;
+    const int64_t k0 = (tb % nks) * kslab, k1 = min(ps.K, k0 + kslab);
+    int m = 0;
+    if (r < ps.R) {
+      const int64_t ro = oz_row_off(ps, r);
+      for (int64_t k = k0 + ty; k < k1; k += 8) m = max(m, biased_exp(src[ro + oz_col_off(ps, k)]));
+    }
+    red[ty][tx] = m;
+    __syncthreads();
+    if (ty == 0) {
+      for (int j = 1; j < 8; ++j) m = max(m, red[j][tx]);
+      if (r < ps.R && m > 0) atomicMax(ex + r, m);
+    }
+    __syncthreads();
+  }
+}
+
+// The S balanced base-64 digits of y = x 2^-e (|x| < 2^e): the integer
+// Z = round(|y| 64^S) is cut into digits d_S..d_2 in [-32, 32) (carrying into
+// the next one) and d_1 = the rest, 0..64; all signed like x.  Integer
+// arithmetic only; |y - sum_s d_s 64^-s| <= 64^-S / 2.
+__device__ __forceinline__ void oz_digits(double x, int e, int S, __nv_bfloat16* d) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int be = (int)((bits >> 52) & 0x7FF);
+  unsigned long long Z = 0;
+  if (be != 0) {
+    const unsigned long long m = (bits & ((1ull << 52) - 1)) | (1ull << 52);   // |x| = m 2^(be - 1075)
+    const int sh = 1075 + e - 6 * S - be;                                      // Z = m 2^-sh, sh > 0
+    if (sh <= 0) Z = m << (-sh);
+    else if (sh < 64) Z = (m >> sh) + ((m >> (sh - 1)) & 1ull);
+  }
+  const bool neg = (bits >> 63) != 0;
+  for (int s = S - 1; s >= 1; --s) {
+    int r = (int)(Z & 63ull);
+    Z >>= 6;
+    if (r >= 32) { r -= 64; Z += 1; }
+    d[s] = __float2bfloat16_rn((float)(neg ? -r : r));
+  }
+  d[0] = __float2bfloat16_rn((float)(neg ? -(int)Z : (int)Z));
+}
+
+constexpr int OZ_MAXS = 8;
+
+// dst[r][s*Kpad + k]: row-major walk, 4 consecutive k of one row per thread
+__global__ void oz_pack_rows_kernel(const double* __restrict__ src, PackSpec ps, int S, int64_t Kpad,
+                                    const int* __restrict__ ex, __nv_bfloat16* __restrict__ dst) {
+  const int64_t kq = Kpad / 4;
+  const int64_t total = ps.R * kq;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / kq, k0 = (t - r * kq) * 4;
+    __nv_bfloat16* drow = dst + r * (S * Kpad);
+    __nv_bfloat16 dg[4][OZ_MAXS];
+    const int e = oz_row_exp(ex[r]);
+    const int64_t ro = oz_row_off(ps, r);
+    for (int qq = 0; qq < 4; ++qq) {
+      const int64_t k = k0 + qq;
+      oz_digits(k < ps.K ? src[ro + oz_col_off(ps, k)] : 0.0, e, S, dg[qq]);
+    }
+    for (int s = 0; s < S; ++s) {
+      __nv_bfloat162 v0 = __halves2bfloat162(dg[0][s], dg[1][s]);
+      __nv_bfloat162 v1 = __halves2bfloat162(dg[2][s], dg[3][s]);
+      uint2 u;
+      u.x = *reinterpret_cast<uint32_t*>(&v0);
+      u.y = *reinterpret_cast<uint32_t*>(&v1);
+      *reinterpret_cast<uint2*>(drow + s * Kpad + k0) = u;
+    }
+  }
+}
+
+// transposing walk through a 32 x 32 tile (row index faster in the source)
+__global__ void oz_pack_tiles_kernel(const double* __restrict__ src, PackSpec ps, int S, int64_t Kpad,
+                                     const int* __restrict__ ex, __nv_bfloat16* __restrict__ dst) {
+  __shared__ double tile[32][33];
+  const int64_t ntr = (ps.R + 31) / 32, ntk = Kpad / 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
+  for (int64_t tb = blockIdx.x; tb < ntr * ntk; tb += gridDim.x) {
+    const int64_t r0 = (tb / ntk) * 32, k0 = (tb % ntk) * 32;
+    __syncthreads();
+    for (int j = 0; j < 4; ++j) {
+      const int kk = ty + 8 * j;
+      const int64_t r = r0 + tx, k = k0 + kk;
+      tile[kk][tx] = (r < ps.R && k < ps.K) ? src[oz_row_off(ps, r) + oz_col_off(ps, k)] : 0.0;
+    }
+    __syncthreads();
+    for (int j = 0; j < 4; ++j) {
+      const int rr = ty + 8 * j;
+      const int64_t r = r0 + rr, k = k0 + tx;
+      if (r >= ps.R) continue;
+      __nv_bfloat16 dg[OZ_MAXS];
+      oz_digits(tile[tx][rr], oz_row_exp(ex[r]), S, dg);
+      __nv_bfloat16* d = dst + r * (S * Kpad) + k;
+      for (int s = 0; s < S; ++s) d[s * Kpad] = dg[s];
+    }
+  }
+}
+
+std::once_flag g_oz_attr;
+
+}  // namespace
+
+int64_t oz_kpad(int64_t K) { return ((K + OZ_BK - 1) / OZ_BK) * OZ_BK; }
+
+void pack_oz(const double* src, const PackSpec& ps, int S, __nv_bfloat16* dst, int* ex, cudaStream_t s) {
+  if (ps.R <= 0 || ps.K <= 0) return;
+  if (S < 1 || S > OZ_MAXS) fail(FCC_ERR_BAD_ARG, "bad slice count");
+  const int64_t Kpad = oz_kpad(ps.K);
+  const int pidx = prof_begin(s);
+  struct End { cudaStream_t s; int i; double b; ~End() { prof_end(s, i, PROF_PACK, b); } } pend{s, pidx,
+      2.0 * (double)ps.R * (double)ps.K * 8.0 + (double)ps.R * (double)(S * Kpad) * 2.0};
+  FCC_CUDA(cudaMemsetAsync(ex, 0, sizeof(int) * ps.R, s));
+  const int64_t kfast = std::llabs(ps.kd3 > 1 ? ps.ks3 : (ps.kd2 > 1 ? ps.ks2 : ps.ks1));
+  const int64_t rfast = std::llabs(ps.rd3 > 1 ? ps.rs3 : (ps.rd2 > 1 ? ps.rs2 : ps.rs1));
+  const bool tiles = rfast < kfast && ps.R >= 32;
+  // k-slabs so that the exponent pass has enough independent work
+  const int64_t want = 152 * 64;
+  const int64_t units = tiles ? (ps.R + 31) / 32 : ps.R;
+  int64_t kslab = ps.K;
+  if (units < want) kslab = std::max<int64_t>(256, (ps.K * units + want - 1) / want);
+  const int64_t nks = (ps.K + kslab - 1) / kslab;
+  if (tiles) {
+    oz_exp_tiles_kernel<<<(unsigned)std::min<int64_t>(units * nks, 152 * 32), 256, 0, s>>>(src, ps, kslab, ex);
+    FCC_CHECK_LAUNCH();
+    const int64_t nt = ((ps.R + 31) / 32) * (Kpad / 32);
+    oz_pack_tiles_kernel<<<(unsigned)std::min<int64_t>(nt, 152 * 16), 256, 0, s>>>(src, ps, S, Kpad, ex, dst);
+    FCC_CHECK_LAUNCH();
+  } else {
+    const int64_t warps = units * nks;
+    oz_exp_rows_kernel<<<(unsigned)std::min<int64_t>((warps + 7) / 8, 152 * 32), 256, 0, s>>>(src, ps, kslab, ex);
+    FCC_CHECK_LAUNCH();
+    const int64_t tot = ps.R * (Kpad / 4);
+    oz_pack_rows_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 152 * 32), 256, 0, s>>>(src, ps, S, Kpad, ex,
+                                                                                                 dst);
+    FCC_CHECK_LAUNCH();
+  }
+}
+
+void gemm_oz(const __nv_bfloat16* A, int64_t a_rows, const int* exA, const __nv_bfloat16* B, int64_t b_rows,
+             const int* exB, int64_t Kpad, int G, const EpiMap& ep, int* err, cudaStream_t s) {
+  if (ep.M <= 0 || ep.N <= 0) return;
+  if (ep.mode != EPI_F64) fail(FCC_ERR_BAD_ARG, "exact-slice products write FP64 only");
+  if (G < 2 || G > OZ_MAXS + 1) fail(FCC_ERR_BAD_ARG, "bad exact-slice group count");
+  if (Kpad <= 0 || Kpad % OZ_BK) fail(FCC_ERR_BAD_ARG, "bad padded K");
+  if (a_rows < ep.M || b_rows < ep.N) fail(FCC_ERR_BAD_ARG, "packed operands smaller than the output");
+  const int S = G - 1;
+  const int nkb = (int)(Kpad / OZ_BK);
+  std::call_once(g_oz_attr, []() {
+    cudaFuncSetAttribute(gemm_oz_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
+  });
+  const OzPairs pr = make_pairs(G);
+  CUtensorMap ta = tma_map_bf16(A, a_rows, S * Kpad, OZ_BM);
+  CUtensorMap tb = tma_map_bf16(B, b_rows, S * Kpad, OZ_BN);
+  const int64_t tm = (ep.M + OZ_BM - 1) / OZ_BM, tn = (ep.N + OZ_BN - 1) / OZ_BN;
+  const int64_t tiles = tm * tn;
+  const int total = pr.n * nkb;
+  // split the step sequence over CTAs when that shortens the last wave
+  int splits = 1;
+  double best = 1e300;
+  for (int sp = 1; sp <= 64 && sp * OZ_CH <= total; ++sp) {
+    const double waves = std::ceil((double)(tiles * sp) / 152.0);
+    const double t = waves / sp;
+    if (t < best * 0.97) { best = t; splits = sp; }
+  }
+  const int per = (total + splits - 1) / splits;
+  splits = (total + per - 1) / per;
+  // no loads of C in the kernel: beta = 0 and one K range store, otherwise C
+  // is scaled by beta first (not for beta = 1) and the kernel reduces into it
+  EpiMap e2 = ep;
+  e2.atomic = (splits > 1 || ep.beta != 0.0) ? 1 : 0;
+  if (e2.atomic && ep.beta != 1.0) scale_output(ep, ep.beta, s);
+  dim3 grid((unsigned)tm, (unsigned)tn, (unsigned)splits);
+  if (grid.y > 65535 || grid.x > 2147483647u) fail(FCC_ERR_BAD_ARG, "exact-slice grid too large");
+  const int pidx = prof_begin(s);
+  gemm_oz_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(ta, tb, nkb, (int)Kpad, pr, per, exA, exB, G, e2, err);
+  FCC_CHECK_LAUNCH();
+  prof_end(s, pidx, PROF_OZ, ep.work > 0 ? ep.work : 2.0 * (double)ep.M * (double)ep.N * (double)(Kpad * pr.n));
+}
+
+}  // namespace fcc

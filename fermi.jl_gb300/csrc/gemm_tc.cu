@@ -20,15 +20,17 @@
 #include <mutex>
 
 #include "fcc_tc.cuh"
+#include "fcc_tcgen05.cuh"
 
 namespace fcc {
 
 namespace {
 
+using namespace tc5;
+
 constexpr int BM = 128;
 constexpr int BK = 64;                       // one 128-byte swizzle atom of bf16 per row
 constexpr int TC_THREADS = 192;              // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
-constexpr uint64_t WAIT_NS = 2000000000ull;  // every mbarrier wait gives up after 2 s
 
 template <int BN>
 struct TcCfg {
@@ -38,64 +40,6 @@ struct TcCfg {
   static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024;  // + alignment slack
 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ uint64_t globaltimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Bounded wait on an mbarrier phase; false after WAIT_NS.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  uint64_t t0 = 0;
-  for (uint32_t it = 0;; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if (it == 0) t0 = globaltimer();
-    else if ((it & 63) == 0 && globaltimer() - t0 > WAIT_NS) return false;
-  }
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* tm, int32_t x, int32_t y, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar)
-      : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle,
-// 8-row groups 1024 bytes apart (SBO), fixed version bits 46-48 = 0b001.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;             // SWIZZLE_128B
-  return d;
-}
-
-// Instruction descriptor, kind::f16: D F32, A and B BF16, both K-major.
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
 
 // hi, mid, lo bf16 pieces of x (x - hi - mid - lo ~ 2^-25 |x|)
 __device__ __forceinline__ void split3(double x, __nv_bfloat16 (&lv)[3]) {
@@ -325,7 +269,7 @@ __global__ void pack_rows_kernel(const double* __restrict__ src, PackSpec ps, __
       const int64_t ro = row_off(ps, r);
       __nv_bfloat16 lv[4][3];
       const int cnt = (int)min((int64_t)4, ps.K - k0);
-      for (int q = 0; q < 4; ++q) split3(q < cnt ? src[ro + col_off(ps, k0 + q)] : 0.0, lv[q]);
+      for (int q = 0; q < 4; ++q) split3(q < cnt ? ps.scale * src[ro + col_off(ps, k0 + q)] : 0.0, lv[q]);
       for (int p = 0; p < ps.P; ++p) {
         const int lev = (ps.code >> (2 * p)) & 3;
         __nv_bfloat16* d = drow + p * ps.K + k0;
@@ -362,7 +306,7 @@ __global__ void pack_tiles_kernel(const double* __restrict__ src, PackSpec ps, _
     for (int j = 0; j < 4; ++j) {
       const int kk = ty + 8 * j;
       const int64_t r = r0 + tx, k = k0 + kk;
-      tile[kk][tx] = (r < ps.R && k < ps.K) ? src[row_off(ps, r) + col_off(ps, k)] : 0.0;
+      tile[kk][tx] = (r < ps.R && k < ps.K) ? ps.scale * src[row_off(ps, r) + col_off(ps, k)] : 0.0;
     }
     __syncthreads();
     for (int j = 0; j < 4; ++j) {
@@ -475,6 +419,17 @@ void launch_tc(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __n
 }  // namespace
 
 int64_t packed_kp(int64_t K, int P) { return ((P * K + BK - 1) / BK) * BK; }
+
+CUtensorMap tma_map_bf16(const __nv_bfloat16* base, int64_t rows, int64_t cols, int box_rows) {
+  return make_map(base, rows, cols, box_rows);
+}
+
+void scale_output(const EpiMap& ep, double beta, cudaStream_t s) {
+  const int64_t tot = ep.M * ep.N;
+  if (tot <= 0) return;
+  scale_out_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 152 * 16), 256, 0, s>>>(ep, beta);
+  FCC_CHECK_LAUNCH();
+}
 
 void pack_split(const double* src, const PackSpec& ps, __nv_bfloat16* dst, cudaStream_t s) {
   if (ps.R <= 0 || ps.K <= 0) return;

@@ -1,96 +1,149 @@
 // RCCSD(T) in the mixed form: split-BF16 tensor-core contractions with FP32
-// accumulation for W; V and the permutation sums in FP32; the denominators,
-// the division and the energy reduction in FP64.
+// accumulation for W; V, the permutation sums and the quotient by the
+// denominator in FP32; the denominators and the energy reduction in FP64.
 //
-// Same algorithm as the FP64 form (PerturbativeTriples/ijk.jl:20-149), batched
-// for the tensor cores: for every pair i >= j the intermediates W_k for all
-// k <= j are built together, so each of the twelve contractions of
-// ijk.jl:109-114 is ONE GEMM whose N (or M) dimension runs over k.  Every
-// operand is split and packed once per (T) call into the row layouts the
-// GEMMs read with 2-D TMA boxes:
-//   OVp[x][y][z][d]   = (xy|zd)         (A and B patterns)
-//   OVpT[x][y][z][d]  = (xz|yd)         (B)
-//   P1[x][k][c][d]    = t(k,x,c,d)      (B)
-//   P2[x][k][b][d]    = t(x,k,b,d)      (A)
-//   P3[x][c][a][l]    = t(x,l,c,a)      (A and B)
-//   P3T[x][y][z][l]   = t(x,l,z,y)      (B)
-//   OOq[x][y][a][l]   = (ly|xa)         (A)
-//   OOr[y][x][a][l]   = (ly|xa)         (B)
-// and each GEMM's epilogue scatters into W[k][a][b][c] (FP32) with the index
-// permutation of its term; every GEMM is oriented so its N index ends in c.
+// Same algorithm as the FP64 form (PerturbativeTriples/ijk.jl:20-149),
+// arranged for the tensor cores.  For a pair i >= j and a run of k <= j, the
+// twelve contractions of ijk.jl:109-114 are three grouped products (one per
+// lone virtual index, gemm_t3.cu), written once as G_g[k][pair][lone]:
+//   W_ijk(a,b,c) = G0[k][a][b][c] + G1[k][a][c][b] + G2[k][b][c][a].
+// The energy kernel works on 8 x 8 x 8 sub-cubes (a-, b-, c-blocks A >= B >= C):
+// it stages the sub-blocks of G0, G1, G2 for the six permutations of the
+// sub-cube in shared memory with coalesced loads, forms W there, and
+// evaluates every a >= b >= c of the sub-cube from shared memory.
+//
+// Packed split-BF16 operands (rows x K, built once per call):
+//   OVA [x][y][z] = (xy|zd)      OVTA[x][y][z] = (xz|yd)        (A side, K = d)
+//   P3A [x][y][z] = -t(x,l,y,z)  P3TA[x][y][z] = -t(x,l,z,y)    (A side, K = l)
+//   P1B [x][k][c] = t(k,x,c,d)   P2B [x][k][b] = t(x,k,b,d)     (B side, K = d)
+//   OORB[y][x][a] = (ly|xa)                                     (B side, K = l)
 #include <cmath>
+#include <cstring>
+#include <vector>
 
 #include "fcc_ctx.cuh"
+#include "fcc_t3.cuh"
 
 namespace fcc {
 
 namespace {
 
-constexpr int EB = 256;
-constexpr int EBLOCKS = 152;
+constexpr int ET = 8;          // sub-cube edge of the energy kernel
+constexpr int ETH = 256;       // threads per energy block
 
-__device__ __forceinline__ double warp_sum(double x) {
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-  return x;
-}
+struct TileTri {
+  int16_t a, b, c, pad;
+};
 
-// Energy of the triplets (i, j, k), k = 0..nk-1, from W[k][a][b][c] (FP32).
-// V = W + t1_ia (jb|kc) + (ia|kc) t1_jb + (ia|jb) t1_kc and the six-fold
-// permutation sums are FP32 (W itself is an FP32-accumulated split-BF16
-// result); the orbital-energy denominators, the division and the reduction
-// are FP64.  part[k*gridDim.x + block] accumulates across calls in a fixed
-// order.
-__global__ void __launch_bounds__(EB) triples_energy_batch_kernel(const float* __restrict__ Wb,
-                                                                  const float* __restrict__ t1f,
-                                                                  const float* __restrict__ ovovf,
-                                                                  const double* __restrict__ eps, int o, int v,
-                                                                  int i, int j, int k0, double* part) {
-  const int k = k0 + blockIdx.y;
+// Energy of the triplets (i, j, k0 + blockIdx.y) on the sub-cube
+// tiles[blockIdx.x] (tile blocks A >= B >= C).  part[k * ntiles + tile]
+// accumulates over the calls in a fixed order.
+__global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
+    const float* __restrict__ G, int nk, const TileTri* __restrict__ tiles, int ntiles, const float* __restrict__ t1f,
+    const float* __restrict__ ovovf, const double* __restrict__ eps, int o, int v, int i, int j, int k0,
+    double* __restrict__ part) {
+  __shared__ float Wt[6][ET][ET][ET + 1];   // W on the six permutations of the sub-cube
+  __shared__ float Mjk[3][3][ET][ET + 1];   // (j y|k z) for y in block r1, z in block r2
+  __shared__ float Mik[3][3][ET][ET + 1];
+  __shared__ float Mij[3][3][ET][ET + 1];
+  __shared__ float T1[3][3][ET];            // t1 of i, j, k on block r
+  __shared__ double epsv[3][ET];
+  __shared__ double Dab[ET][ET];            // e_i + e_j + e_k - e_a - e_b
+  __shared__ double red[ETH / 32];
+  const int kq = blockIdx.y, k = k0 + kq;
   if (i == j && j == k) return;
-  const float* W = Wb + (int64_t)blockIdx.y * v * v * v;
-  const int64_t mstr = (int64_t)o * v;
-  const float* Mjk = ovovf + ((int64_t)j * v * o + k) * v;
-  const float* Mik = ovovf + ((int64_t)i * v * o + k) * v;
-  const float* Mij = ovovf + ((int64_t)i * v * o + j) * v;
-  const float* t1i = t1f + (int64_t)i * v;
-  const float* t1j = t1f + (int64_t)j * v;
-  const float* t1k = t1f + (int64_t)k * v;
-  auto Wat = [&](int x, int y, int z) -> float { return W[((int64_t)x * v + y) * v + z]; };
-  auto Vat = [&](int x, int y, int z, float w) -> float {
-    return w + t1i[x] * Mjk[(int64_t)y * mstr + z] + Mik[(int64_t)x * mstr + z] * t1j[y] +
-           Mij[(int64_t)x * mstr + y] * t1k[z];
-  };
-  const double Dijk = eps[i] + eps[j] + eps[k];
-  const double* fv = eps + o;
-  const int64_t npair = (int64_t)v * (v + 1) / 2;
-  double acc = 0.0;
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npair; p += (int64_t)gridDim.x * blockDim.x) {
-    int a = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
-    while ((int64_t)a * (a + 1) / 2 > p) --a;
-    while ((int64_t)(a + 1) * (a + 2) / 2 <= p) ++a;
-    const int b = (int)(p - (int64_t)a * (a + 1) / 2);
-    const double Dab = Dijk - fv[a] - fv[b];
-    for (int c = 0; c <= b; ++c) {
-      const float Wabc = Wat(a, b, c), Wacb = Wat(a, c, b), Wbac = Wat(b, a, c);
-      const float Wbca = Wat(b, c, a), Wcab = Wat(c, a, b), Wcba = Wat(c, b, a);
-      const float Vabc = Vat(a, b, c, Wabc), Vacb = Vat(a, c, b, Wacb), Vbac = Vat(b, a, c, Wbac);
-      const float Vbca = Vat(b, c, a, Wbca), Vcab = Vat(c, a, b, Wcab), Vcba = Vat(c, b, a, Wcba);
-      const float X = Wabc * Vabc + Wacb * Vacb + Wbac * Vbac + Wbca * Vbca + Wcab * Vcab + Wcba * Vcba;
-      const float Y = Vabc + Vbca + Vcab;
-      const float Z = Vacb + Vbac + Vcba;
-      const float Ef = (Y - 2.0f * Z) * (Wabc + Wbca + Wcab) + (Z - 2.0f * Y) * (Wacb + Wbac + Wcba) + 3.0f * X;
-      const double wgt = 1.0 + (a == b) + (b == c);
-      acc += (double)Ef / ((Dab - fv[c]) * wgt);
-    }
+  const TileTri tt = tiles[blockIdx.x];
+  const int oa = tt.a * ET, ob = tt.b * ET, oc = tt.c * ET;
+  auto org = [&](int r) { return r == 0 ? oa : (r == 1 ? ob : oc); };
+  const int64_t v2 = (int64_t)v * v, v3 = v2 * v;
+  const float* G0 = G + ((int64_t)0 * nk + kq) * v3;   // [a][b][c]
+  const float* G1 = G + ((int64_t)1 * nk + kq) * v3;   // [a][c][b]
+  const float* G2 = G + ((int64_t)2 * nk + kq) * v3;   // [b][c][a]
+  // permutation p: roles (rx, ry, rz) of the sub-cube blocks, 2 bits each:
+  // (0,1,2) (0,2,1) (1,0,2) (1,2,0) (2,0,1) (2,1,0)
+  constexpr uint64_t PRC = (0ull | 1ull << 2 | 2ull << 4) | (0ull | 2ull << 2 | 1ull << 4) << 8 |
+                           (1ull | 0ull << 2 | 2ull << 4) << 16 | (1ull | 2ull << 2 | 0ull << 4) << 24 |
+                           (2ull | 0ull << 2 | 1ull << 4) << 32 | (2ull | 1ull << 2 | 0ull << 4) << 40;
+  auto role = [](int p, int r) { return (int)((PRC >> (8 * p + 2 * r)) & 3); };
+  const int t = threadIdx.x;
+
+  // ---- stage W = G0[x][y][z] + G1[x][z][y] + G2[y][z][x] in three passes,
+  // each with its thread order along the source's stride-1 index
+  for (int e = t; e < 6 * ET * ET * ET; e += ETH) {
+    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
+    const int x = r / (ET * ET), y = (r / ET) % ET, z = r % ET;   // z fastest
+    const int X = org(role(p, 0)) + x, Y = org(role(p, 1)) + y, Z = org(role(p, 2)) + z;
+    Wt[p][x][y][z] = (X < v && Y < v && Z < v) ? G0[((int64_t)X * v + Y) * v + Z] : 0.0f;
   }
-  __shared__ double sm[EB / 32];
-  acc = warp_sum(acc);
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  for (int e = t; e < 6 * ET * ET * ET; e += ETH) {
+    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
+    const int x = r / (ET * ET), z = (r / ET) % ET, y = r % ET;   // y fastest
+    const int X = org(role(p, 0)) + x, Y = org(role(p, 1)) + y, Z = org(role(p, 2)) + z;
+    if (X < v && Y < v && Z < v) Wt[p][x][y][z] += G1[((int64_t)X * v + Z) * v + Y];
+  }
+  __syncthreads();
+  for (int e = t; e < 6 * ET * ET * ET; e += ETH) {
+    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
+    const int y = r / (ET * ET), z = (r / ET) % ET, x = r % ET;   // x fastest
+    const int X = org(role(p, 0)) + x, Y = org(role(p, 1)) + y, Z = org(role(p, 2)) + z;
+    if (X < v && Y < v && Z < v) Wt[p][x][y][z] += G2[((int64_t)Y * v + Z) * v + X];
+  }
+  // ---- (i y|j z)-type integrals and t1 on the blocks
+  const int64_t mstr = (int64_t)o * v;
+  for (int e = t; e < 9 * ET * ET; e += ETH) {
+    const int rr = e / (ET * ET), q = e % (ET * ET);
+    const int r1 = rr / 3, r2 = rr % 3, y = q / ET, z = q % ET;
+    const int Y = org(r1) + y, Z = org(r2) + z;
+    const bool in = Y < v && Z < v;
+    // ovovf[p][y][q][z] = (p y|q z), row stride o*v
+    Mjk[r1][r2][y][z] = in ? ovovf[((int64_t)j * v + Y) * mstr + (int64_t)k * v + Z] : 0.0f;
+    Mik[r1][r2][y][z] = in ? ovovf[((int64_t)i * v + Y) * mstr + (int64_t)k * v + Z] : 0.0f;
+    Mij[r1][r2][y][z] = in ? ovovf[((int64_t)i * v + Y) * mstr + (int64_t)j * v + Z] : 0.0f;
+  }
+  if (t < 3 * ET) {
+    const int r = t / ET, x = t % ET, X = org(r) + x;
+    T1[0][r][x] = X < v ? t1f[(int64_t)i * v + X] : 0.0f;
+    T1[1][r][x] = X < v ? t1f[(int64_t)j * v + X] : 0.0f;
+    T1[2][r][x] = X < v ? t1f[(int64_t)k * v + X] : 0.0f;
+    epsv[r][x] = X < v ? eps[o + X] : 0.0;
+  }
+  __syncthreads();
+  if (t < ET * ET) Dab[t / ET][t % ET] = eps[i] + eps[j] + eps[k] - epsv[0][t / ET] - epsv[1][t % ET];
+  __syncthreads();
+
+  // V(x,y,z) for x in block rx at lx etc.: W + t1_ix (jy|kz) + (ix|kz) t1_jy + (ix|jy) t1_kz
+  auto V = [&](int rx, int lx, int ry, int ly, int rz, int lz, float w) -> float {
+    return w + T1[0][rx][lx] * Mjk[ry][rz][ly][lz] + Mik[rx][rz][lx][lz] * T1[1][ry][ly] +
+           Mij[rx][ry][lx][ly] * T1[2][rz][lz];
+  };
+  double acc = 0.0;
+  for (int e = t; e < ET * ET * ET; e += ETH) {
+    const int la = e / (ET * ET), lb = (e / ET) % ET, lc = e % ET;
+    const int a = oa + la, b = ob + lb, c = oc + lc;
+    if (a >= v || b >= v || c >= v || b > a || c > b) continue;
+    const float Wabc = Wt[0][la][lb][lc], Wacb = Wt[1][la][lc][lb], Wbac = Wt[2][lb][la][lc];
+    const float Wbca = Wt[3][lb][lc][la], Wcab = Wt[4][lc][la][lb], Wcba = Wt[5][lc][lb][la];
+    const float Vabc = V(0, la, 1, lb, 2, lc, Wabc), Vacb = V(0, la, 2, lc, 1, lb, Wacb);
+    const float Vbac = V(1, lb, 0, la, 2, lc, Wbac), Vbca = V(1, lb, 2, lc, 0, la, Wbca);
+    const float Vcab = V(2, lc, 0, la, 1, lb, Wcab), Vcba = V(2, lc, 1, lb, 0, la, Wcba);
+    const float X = Wabc * Vabc + Wacb * Vacb + Wbac * Vbac + Wbca * Vbca + Wcab * Vcab + Wcba * Vcba;
+    const float Y = Vabc + Vbca + Vcab;
+    const float Z = Vacb + Vbac + Vcba;
+    const float Ef = (Y - 2.0f * Z) * (Wabc + Wbca + Wcab) + (Z - 2.0f * Y) * (Wacb + Wbac + Wcba) + 3.0f * X;
+    // denominator in FP64; the quotient of the FP32 Ef in FP32 (the FP64 pipe
+    // is 1/64 rate: an FP64 division per (a,b,c) bounded this kernel)
+    const double D = Dab[la][lb] - epsv[2][lc];
+    const float wgt = 1.0f + (float)(a == b) + (float)(b == c);
+    acc += (double)__fdiv_rn(Ef, (float)D * wgt);
+  }
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((t & 31) == 0) red[t >> 5] = acc;
+  __syncthreads();
+  if (t == 0) {
     double s = 0.0;
-    for (int w = 0; w < EB / 32; ++w) s += sm[w];
-    part[(int64_t)k * gridDim.x + blockIdx.x] += (2.0 - (i == j) - (j == k)) * s;
+    for (int w = 0; w < ETH / 32; ++w) s += red[w];
+    part[(int64_t)k * ntiles + blockIdx.x] += (2.0 - (i == j) - (j == k)) * s;
   }
 }
 
@@ -107,28 +160,19 @@ __global__ void sum_parts_kernel(const double* part, int64_t n, double* out) {
   }
 }
 
-// 3-level row spec helper for packing: rows (x, y, z) with strides, K with stride.
-PackSpec pspec(int64_t d1, int64_t d2, int64_t d3, int64_t s1, int64_t s2, int64_t s3, int64_t K, int64_t ks) {
+// 3-level row spec for packing: rows (x, y, z) with strides, K with stride.
+PackSpec pspec(int64_t d1, int64_t d2, int64_t d3, int64_t s1, int64_t s2, int64_t s3, int64_t K, int64_t ks,
+               uint32_t code, double scale = 1.0) {
   PackSpec p;
   p.R = d1 * d2 * d3;
   p.K = K;
   p.Kp = packed_kp(K, SPLIT3.P);
   p.P = SPLIT3.P;
-  p.code = SPLIT3.code_a;
+  p.code = code;
+  p.scale = scale;
   p.rd2 = d2; p.rd3 = d3; p.rs1 = s1; p.rs2 = s2; p.rs3 = s3;
   p.kd2 = 1; p.kd3 = K; p.ks1 = 0; p.ks2 = 0; p.ks3 = ks;
   return p;
-}
-
-// Epilogue map: m = (m1, m2, m3) and n = (n1, n2, n3) with output strides.
-EpiMap emap(int64_t M, int64_t md2, int64_t md3, int64_t ms1, int64_t ms2, int64_t ms3, int64_t N, int64_t nd2,
-            int64_t nd3, int64_t ns1, int64_t ns2, int64_t ns3, double alpha, double beta, float* C) {
-  EpiMap e;
-  e.M = M; e.md2 = md2; e.md3 = md3; e.ms1 = ms1; e.ms2 = ms2; e.ms3 = ms3;
-  e.N = N; e.nd2 = nd2; e.nd3 = nd3; e.ns1 = ns1; e.ns2 = ns2; e.ns3 = ns3;
-  e.alpha = alpha; e.beta = beta; e.C = C; e.mode = EPI_F32;
-  e.work = 0.0;
-  return e;
 }
 
 }  // namespace
@@ -136,49 +180,92 @@ EpiMap emap(int64_t M, int64_t md2, int64_t md3, int64_t ms1, int64_t ms2, int64
 double triples_mixed(fcc_ctx* c) {
   cudaStream_t s = c->stream;
   const int64_t o = c->o, v = c->v, Q = c->Q, n = c->n;
+  const int bn = t3_bn((int)v);
+  if (bn == 0) fail(FCC_ERR_BAD_ARG, "the mixed (T) needs v <= 256");
   TView B = rm(c->B.p, {Q, n, n});
   TView Boo = slice(slice(B, 1, 0, o), 2, 0, o);
   TView Bov = slice(slice(B, 1, 0, o), 2, o, v);
   TView Bvv = slice(slice(B, 1, o, v), 2, o, v);
-  // FP64 integrals, then their split-BF16 packed copies
+  if (!c->dev_err.p) c->dev_err.alloc(1);
+  FCC_CUDA(cudaMemsetAsync(c->dev_err.p, 0, sizeof(int), s));
+  int* err = c->dev_err.p;
+  // (ia|bd) and (li|jb) from the factors by exact-slice products
   DBuf<double> ovvv, ooov;
   ovvv.alloc(o * v * v * v);
   ooov.alloc(o * o * o * v);
-  einsum(1.0, "Qia,Qbd->iabd", Bov, Bvv, 0.0, rm(ovvv.p, {o, v, v, v}), s);
-  einsum(1.0, "Qli,Qjb->lijb", Boo, Bov, 0.0, rm(ooov.p, {o, o, o, v}), s);
+  {
+    TcScope scope(&c->tc);
+    c->tc.enabled = true;
+    c->tc.exact = true;
+    c->tc.err = err;
+    einsum(1.0, "Qia,Qbd->iabd", Bov, Bvv, 0.0, rm(ovvv.p, {o, v, v, v}), s);
+    einsum(1.0, "Qli,Qjb->lijb", Boo, Bov, 0.0, rm(ooov.p, {o, o, o, v}), s);
+    c->tc.exact = false;
+  }
   const int64_t v2 = v * v, v3 = v2 * v;
-  const int64_t Kv = packed_kp(v, SPLIT3.P), Ko = packed_kp(o, SPLIT3.P);
-  auto packA = [&](const double* src, PackSpec ps, __nv_bfloat16* dst) { ps.code = SPLIT3.code_a; pack_split(src, ps, dst, s); };
-  auto packB = [&](const double* src, PackSpec ps, __nv_bfloat16* dst) { ps.code = SPLIT3.code_b; pack_split(src, ps, dst, s); };
-  DBuf<__nv_bfloat16> OVpA, OVpB, OVpTB, P1, P2A, P3, P3A, P3T, OOq, OOrB;
-  PackSpec ps_ov = pspec(o, v, v, v3, v2, v, v, 1);            // OVp[x][y][z]  = (xy|zd)
-  PackSpec ps_ovt = pspec(o, v, v, v3, v, v2, v, 1);           // OVpT[x][y][z] = (xz|yd)
-  OVpA.alloc(ps_ov.R * Kv); OVpB.alloc(ps_ov.R * Kv); OVpTB.alloc(ps_ovt.R * Kv);
-  packA(ovvv.p, ps_ov, OVpA.p);
-  packB(ovvv.p, ps_ov, OVpB.p);
-  packB(ovvv.p, ps_ovt, OVpTB.p);
-  ovvv.release();
+  const uint32_t CA = SPLIT3.code_a, CB = SPLIT3.code_b;
   const double* t2 = c->t2.p;   // t2[i][j][a][b]: strides o*v2, v2, v, 1
-  PackSpec ps1 = pspec(o, o, v, v2, o * v2, v, v, 1);          // P1[x][k][c]  = t(k,x,c,:)
-  PackSpec ps2 = pspec(o, o, v, o * v2, v2, v, v, 1);          // P2[x][k][b]  = t(x,k,b,:)
-  PackSpec ps3 = pspec(o, v, v, o * v2, v, 1, o, v2);          // P3[x][c][a]  = t(x,l,c,a) over l
-  PackSpec ps3t = pspec(o, v, v, o * v2, 1, v, o, v2);         // P3T[x][y][z] = t(x,l,z,y) over l
-  P1.alloc(ps1.R * Kv); P2A.alloc(ps2.R * Kv); P3.alloc(ps3.R * Ko); P3A.alloc(ps3.R * Ko); P3T.alloc(ps3t.R * Ko);
-  packB(t2, ps1, P1.p);
-  packA(t2, ps2, P2A.p);
-  packB(t2, ps3, P3.p);
-  packA(t2, ps3, P3A.p);
-  packB(t2, ps3t, P3T.p);
-  // ooov[l][y][x][a] = (ly|xa): strides l o2v, y o v, x v, a 1
-  PackSpec psq = pspec(o, o, v, v, o * v, 1, o, o * o * v);    // OOq[x][y][a]
-  PackSpec psr = pspec(o, o, v, o * v, v, 1, o, o * o * v);    // OOr[y][x][a]
-  OOq.alloc(psq.R * Ko); OOrB.alloc(psr.R * Ko);
-  packA(ooov.p, psq, OOq.p);
-  packB(ooov.p, psr, OOrB.p);
+  // ovvv[x][y][z][d] = (xy|zd); ooov[l][y][x][a] = (ly|xa)
+  PackSpec sOVA = pspec(o, v, v, v3, v2, v, v, 1, CA);
+  PackSpec sOVTA = pspec(o, v, v, v3, v, v2, v, 1, CA);
+  PackSpec sP3A = pspec(o, v, v, o * v2, v, 1, o, v2, CA, -1.0);
+  PackSpec sP3TA = pspec(o, v, v, o * v2, 1, v, o, v2, CA, -1.0);
+  PackSpec sP1B = pspec(o, o, v, v2, o * v2, v, v, 1, CB);
+  PackSpec sP2B = pspec(o, o, v, o * v2, v2, v, v, 1, CB);
+  PackSpec sOORB = pspec(o, o, v, o * v, v, 1, o, o * o * v, CB);
+  const PackSpec* specs[7] = {&sOVA, &sOVTA, &sP3A, &sP3TA, &sP1B, &sP2B, &sOORB};
+  const double* srcs[7] = {ovvv.p, ovvv.p, t2, t2, t2, t2, ooov.p};
+  DBuf<__nv_bfloat16> packed[7];
+  for (int q = 0; q < 7; ++q) {
+    packed[q].alloc(specs[q]->R * specs[q]->Kp);
+    pack_split(srcs[q], *specs[q], packed[q].p, s);
+  }
+  ovvv.release();
   ooov.release();
 
-  DBuf<float> Wb, t1f, ovovf;
-  Wb.alloc(std::max<int64_t>(1, std::min<int64_t>(o, (96ll << 20) / (v3 * 4))) * v3);
+  T3Params P;
+  std::memset(&P, 0, sizeof(P));
+  for (int q = 0; q < 7; ++q) P.maps[q] = tma_map_bf16(packed[q].p, specs[q]->R, specs[q]->Kp, q < 4 ? 128 : bn);
+  enum { OVA = 0, OVTA = 1, P3A = 2, P3TA = 3, P1B = 4, P2B = 5, OORB = 6 };
+  enum { SI = 0, SJ = 1, SK = 2 };
+  const int16_t kbv = (int16_t)(sOVA.Kp / 64), kbo = (int16_t)(sP3A.Kp / 64);
+  auto seg = [&](int amap, int asel, int bmap, int b1, int b2) {
+    return T3Seg{(int8_t)amap, (int8_t)asel, (int8_t)bmap, (int8_t)b1, (int8_t)b2, (amap <= OVTA) ? kbv : kbo};
+  };
+  // group 0: rows (a,b), lone c: :109a (ia|bd)t(kj,cd), :110a (jb|ad)t(ki,cd),
+  //          :113b -(li|kc)t(jl,ba), :114b -(lj|kc)t(il,ab)
+  P.seg[0][0] = seg(OVA, SI, P1B, SJ, SK);
+  P.seg[0][1] = seg(OVTA, SJ, P1B, SI, SK);
+  P.seg[0][2] = seg(P3TA, SJ, OORB, SI, SK);
+  P.seg[0][3] = seg(P3A, SI, OORB, SJ, SK);
+  // group 1: rows (a,c), lone b: :111a (kc|ad)t(ji,bd), :113a (ia|cd)t(kj,db),
+  //          :112b -(lk|jb)t(il,ac), :109b -(li|jb)t(kl,ca)
+  P.seg[1][0] = seg(OVTA, SK, P1B, SI, SJ);
+  P.seg[1][1] = seg(OVA, SI, P2B, SJ, SK);
+  P.seg[1][2] = seg(P3A, SI, OORB, SK, SJ);
+  P.seg[1][3] = seg(P3TA, SK, OORB, SI, SJ);
+  // group 2: rows (b,c), lone a: :112a (kc|bd)t(ji,da), :114a (jb|cd)t(ki,da),
+  //          :111b -(lk|ia)t(jl,bc), :110b -(lj|ia)t(kl,cb)
+  P.seg[2][0] = seg(OVTA, SK, P1B, SJ, SI);
+  P.seg[2][1] = seg(OVA, SJ, P2B, SI, SK);
+  P.seg[2][2] = seg(P3A, SJ, OORB, SK, SI);
+  P.seg[2][3] = seg(P3TA, SK, OORB, SJ, SI);
+  P.o = (int)o;
+  P.v = (int)v;
+  P.err = err;
+
+  // sub-cube list of the energy kernel
+  const int nt = (int)((v + ET - 1) / ET);
+  std::vector<TileTri> th;
+  for (int a = 0; a < nt; ++a)
+    for (int b = 0; b <= a; ++b)
+      for (int cc = 0; cc <= b; ++cc) th.push_back(TileTri{(int16_t)a, (int16_t)b, (int16_t)cc, 0});
+  const int ntiles = (int)th.size();
+  DBuf<TileTri> tiles;
+  tiles.alloc(ntiles);
+  FCC_CUDA(cudaMemcpyAsync(tiles.p, th.data(), sizeof(TileTri) * ntiles, cudaMemcpyHostToDevice, s));
+
+  DBuf<float> t1f, ovovf;
   t1f.alloc(o * v);
   ovovf.alloc(o * v * o * v);
   to_f32_kernel<<<152 * 4, 256, 0, s>>>(c->t1.p, t1f.p, o * v);
@@ -186,61 +273,33 @@ double triples_mixed(fcc_ctx* c) {
   to_f32_kernel<<<152 * 16, 256, 0, s>>>(c->ovov.p, ovovf.p, o * v * o * v);
   FCC_CHECK_LAUNCH();
   DBuf<double> part, out;
-  part.alloc(o * EBLOCKS);
+  part.alloc(o * ntiles);
   out.alloc(1);
   part.zero(s);
-  if (!c->dev_err.p) c->dev_err.alloc(1);
-  FCC_CUDA(cudaMemsetAsync(c->dev_err.p, 0, sizeof(int), s));
-  int* err = c->dev_err.p;
-  const int64_t Rov = o * v2, Rp = o * o * v, Rp3 = o * v2;
-  // k is processed in chunks whose W (FP32) fits comfortably in L2, so the
-  // twelve read-modify-write epilogues and the energy pass hit L2
-  const int64_t KC = std::max<int64_t>(1, std::min<int64_t>(o, (96ll << 20) / (v3 * 4)));
-  float* W = Wb.p;
+  // runs of up to KC values of k per launch (G holds 3 * KC * v^3 FP32); long
+  // runs keep the launches large (sizing G to stay in L2, 2 k at (H2O)8, was
+  // slower overall)
+  const int64_t KC = std::max<int64_t>(1, std::min<int64_t>(16, (1ll << 30) / (3 * v3 * 4)));
+  DBuf<float> G;
+  G.alloc(3 * KC * v3);
+  P.G = G.p;
   for (int64_t i = 0; i < o; ++i)
     for (int64_t j = 0; j <= i; ++j)
       for (int64_t k0 = 0; k0 <= j; k0 += KC) {
         const int64_t nk = std::min<int64_t>(KC, j + 1 - k0);
-        // W[k-k0][a][b][c]: strides v3, v2, v, 1.  Operands are oriented so the
-        // GEMM's N index ends in c (stride 1): coalesced epilogue stores.
-        // :109  (ia|bd) t(k,j,c,d)  -  (li|jb) t(k,l,c,a)
-        gemm_bf16x3(OVpA.p, Rov, i * v2, P1.p, Rp, (j * o + k0) * v, Kv,
-                    emap(v2, v, v, 0, v2, v, nk * v, nk, v, 0, v3, 1, 1.0, 0.0, W), err, s);
-        gemm_bf16x3(OOq.p, Rp, (j * o + i) * v, P3T.p, Rp3, k0 * v2, Ko,
-                    emap(v, 1, v, 0, 0, v, nk * v2, v, v, v3, v2, 1, -1.0, 1.0, W), err, s);
-        // :110  (jb|ad) t(k,i,c,d)  -  (lj|ia) t(k,l,c,b)
-        gemm_bf16x3(OVpA.p, Rov, j * v2, P1.p, Rp, (i * o + k0) * v, Kv,
-                    emap(v2, v, v, 0, v, v2, nk * v, nk, v, 0, v3, 1, 1.0, 1.0, W), err, s);
-        gemm_bf16x3(OOq.p, Rp, (i * o + j) * v, P3T.p, Rp3, k0 * v2, Ko,
-                    emap(v, 1, v, 0, 0, v2, nk * v2, v, v, v3, v, 1, -1.0, 1.0, W), err, s);
-        // :111  (kc|ad) t(j,i,b,d)  -  (lk|ia) t(j,l,b,c)
-        gemm_bf16x3(P2A.p, Rp, (j * o + i) * v, OVpTB.p, Rov, k0 * v2, Kv,
-                    emap(v, 1, v, 0, 0, v, nk * v2, v, v, v3, v2, 1, 1.0, 1.0, W), err, s);
-        gemm_bf16x3(OOq.p, Rp, (i * o + k0) * v, P3.p, Rp3, j * v2, Ko,
-                    emap(nk * v, nk, v, 0, v3, v2, v2, v, v, 0, v, 1, -1.0, 1.0, W), err, s);
-        // :112  (kc|bd) t(j,i,d,a)  -  (lk|jb) t(i,l,a,c)
-        gemm_bf16x3(P2A.p, Rp, (i * o + j) * v, OVpTB.p, Rov, k0 * v2, Kv,
-                    emap(v, 1, v, 0, 0, v2, nk * v2, v, v, v3, v, 1, 1.0, 1.0, W), err, s);
-        gemm_bf16x3(OOq.p, Rp, (j * o + k0) * v, P3.p, Rp3, i * v2, Ko,
-                    emap(nk * v, nk, v, 0, v3, v, v2, v, v, 0, v2, 1, -1.0, 1.0, W), err, s);
-        // :113  (ia|cd) t(k,j,d,b)  -  (li|kc) t(j,l,b,a)
-        gemm_bf16x3(P2A.p, Rp, (j * o + k0) * v, OVpB.p, Rov, i * v2, Kv,
-                    emap(nk * v, nk, v, 0, v3, v, v2, v, v, 0, v2, 1, 1.0, 1.0, W), err, s);
-        gemm_bf16x3(P3A.p, Rp3, j * v2, OOrB.p, Rp, (i * o + k0) * v, Ko,
-                    emap(v2, v, v, 0, v, v2, nk * v, nk, v, 0, v3, 1, -1.0, 1.0, W), err, s);
-        // :114  (jb|cd) t(k,i,d,a)  -  (lj|kc) t(i,l,a,b)
-        gemm_bf16x3(P2A.p, Rp, (i * o + k0) * v, OVpB.p, Rov, j * v2, Kv,
-                    emap(nk * v, nk, v, 0, v3, v2, v2, v, v, 0, v, 1, 1.0, 1.0, W), err, s);
-        gemm_bf16x3(P3A.p, Rp3, i * v2, OOrB.p, Rp, (j * o + k0) * v, Ko,
-                    emap(v2, v, v, 0, v2, v, nk * v, nk, v, 0, v3, 1, -1.0, 1.0, W), err, s);
-        dim3 g(EBLOCKS, (unsigned)nk);
+        P.i = (int)i;
+        P.j = (int)j;
+        P.k0 = (int)k0;
+        P.nk = (int)nk;
+        gemm_t3(P, s);
+        dim3 g((unsigned)ntiles, (unsigned)nk);
         const int pe = prof_begin(s);
-        triples_energy_batch_kernel<<<g, EB, 0, s>>>(W, t1f.p, ovovf.p, c->eps.p, (int)o, (int)v, (int)i, (int)j,
-                                                     (int)k0, part.p);
+        triples_energy_tiled_kernel<<<g, ETH, 0, s>>>(G.p, (int)nk, tiles.p, ntiles, t1f.p, ovovf.p, c->eps.p, (int)o,
+                                                      (int)v, (int)i, (int)j, (int)k0, part.p);
         FCC_CHECK_LAUNCH();
         prof_end(s, pe, PROF_TRIPLES, (double)nk * (double)v * (v + 1) * (v + 2) / 6.0);
       }
-  sum_parts_kernel<<<1, 1, 0, s>>>(part.p, o * EBLOCKS, out.p);
+  sum_parts_kernel<<<1, 1, 0, s>>>(part.p, o * ntiles, out.p);
   FCC_CHECK_LAUNCH();
   double et = 0.0;
   int herr = 0;

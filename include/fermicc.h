@@ -45,11 +45,13 @@ extern "C" {
 
 /* arithmetic of the contractions */
 #define FCC_PREC_FP64 0  /* FP64 throughout (the correctness form)                  */
-#define FCC_PREC_MIXED 1 /* split-BF16 tensor-core contractions, FP32 accumulate,   */
-                         /* FP64 denominators/update/DIIS/energies; iterations     */
-                         /* below mixed_switch_rms are corrected by FP64 residual  */
-                         /* evaluations and the run ends on an FP64 residual that  */
-                         /* meets e_conv / max_rms (the FP64 fixed point)          */
+#define FCC_PREC_MIXED 1 /* split-BF16 tensor-core contractions (3 products, FP32  */
+                         /* accumulate) until rms < mixed_switch_rms, then exact-  */
+                         /* slice BF16 products (Ozaki scheme, exact integer       */
+                         /* accumulation) until the criteria hold, then FP64: the  */
+                         /* run ends on an FP64 residual that meets e_conv /       */
+                         /* max_rms (the FP64 fixed point); denominators, update,  */
+                         /* DIIS and energies are FP64 throughout                  */
 
 typedef struct fcc_ctx fcc_ctx;
 
@@ -66,7 +68,7 @@ typedef struct {
   double e_conv;           /* cc_e_conv      (1e-10)                           */
   double max_rms;          /* cc_max_rms     (1e-10)                           */
   double damp;             /* cc_damp_ratio  (0.0)                             */
-  double mixed_switch_rms; /* mixed form: FP64 once rms < this (1e-5)          */
+  double mixed_switch_rms; /* mixed form: leave 3-product BF16 at rms < this (1e-5) */
 } fcc_opts;
 
 /* One line of Fermi's iteration table (RCCSDa.jl:223). */
@@ -74,7 +76,7 @@ typedef struct {
   int32_t ite;
   int32_t diis;      /* 1 if this iteration extrapolated                */
   int32_t precision; /* residual of this iteration: 0 FP64, 1 split-BF16, */
-                     /* 2 split-BF16 + FP64 defect correction           */
+                     /* 2 exact-slice BF16 (Ozaki scheme)                */
   int32_t pad;
   double energy;     /* correlation energy after the iteration          */
   double dE;

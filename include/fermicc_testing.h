@@ -16,9 +16,11 @@ extern "C" {
 
 /* C = alpha * einsum(spec, A, B) + beta * C on device 0 for row-major host
  * tensors (rank <= 4 each).  precision FCC_PREC_FP64 runs the DMMA kernel;
- * FCC_PREC_MIXED forces the three-product split-BF16 tensor-core kernel and
- * 2 the six-product one (error if the contraction cannot be expressed for
- * it).  Returns an fcc status code. */
+ * FCC_PREC_MIXED forces the three-product split-BF16 tensor-core kernel,
+ * 2 the six-product one, 3 the exact-slice (Ozaki) kernel with 7 weight
+ * groups and 10 + G the exact-slice kernel with G groups (2 <= G <= 8)
+ * (error if the contraction cannot be expressed for it).  Returns an fcc
+ * status code. */
 int fcc_test_contract(int32_t precision, const char* spec, const double* A, const int64_t* adims, int32_t arank,
                       const double* B, const int64_t* bdims, int32_t brank, double* C, const int64_t* cdims,
                       int32_t crank, double alpha, double beta);
@@ -34,7 +36,7 @@ void* fcc_stream(const fcc_ctx* ctx);
 /* Opt-in per-class kernel timing with CUDA events on the launching stream:
  * classes 0 FP64 contractions (work = 2MNK flop), 1 tensor-core GEMMs (work =
  * executed BF16 flop), 2 operand packing (work = bytes), 3 updates, 4 (T)
- * energy.  fcc_prof_read fills out[4*c + {0,1,2,3}] = launches, total ms,
+ * energy, 5 exact-slice GEMMs (work = executed BF16 flop).  fcc_prof_read fills out[4*c + {0,1,2,3}] = launches, total ms,
  * work, longest launch ms for c < ncls and clears the log. */
 int fcc_prof_enable(int32_t on);
 int fcc_prof_read(double* out, int32_t ncls);

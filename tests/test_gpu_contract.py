@@ -1,7 +1,10 @@
-"""Single-contraction checks of the two device kernels against numpy.
+"""Single-contraction checks of the device kernels against numpy.
 
 FP64 (DMMA) must agree to round-off; the split-BF16 tensor-core kernel
-(three products, FP32 accumulation) to about 1e-5 of the largest |C|.
+(three products, FP32 accumulation) to about 1e-5 of the largest |C|; the
+exact-slice kernel (Ozaki scheme) to its slice truncation (with 8
+weight groups: ~1e-12 of max|C|) and bit-exactly on operands its slices
+represent exactly.
 """
 import ctypes
 
@@ -71,3 +74,46 @@ def test_six_product_split_contraction(spec, sa, sb, sc):
     ref = np.einsum(spec, A, B)
     err = np.abs(out - ref).max() / np.abs(ref).max()
     assert err < 6e-6, err
+
+
+@pytest.mark.parametrize("spec,sa,sb,sc", CASES)
+def test_exact_slice_contraction(spec, sa, sb, sc):
+    # 8 weight groups (28 slice-pair products): truncation ~2^-42 of
+    # max|A_r| max|B_c| per term, ~1e-12 of max|C| for Gaussian operands
+    rng = np.random.default_rng(3)
+    A, B, C = rng.standard_normal(sa), rng.standard_normal(sb), rng.standard_normal(sc)
+    rc, out = _run(3, spec, A, B, C, 0.7, -1.3)
+    assert rc == 0
+    ref = 0.7 * np.einsum(spec, A, B) - 1.3 * C
+    err = np.abs(out - ref).max() / np.abs(ref).max()
+    assert err < 1e-11, err
+
+
+@pytest.mark.parametrize("G,tol", [(5, 2e-6), (7, 5e-10)])
+def test_exact_slice_groups_set_the_accuracy(G, tol):
+    spec, sa, sb, sc = "mk,nk->mn", (200, 700), (130, 700), (200, 130)
+    rng = np.random.default_rng(4)
+    A, B = rng.standard_normal(sa), rng.standard_normal(sb)
+    rc, out = _run(10 + G, spec, A, B, np.zeros(sc))
+    assert rc == 0
+    ref = A @ B.T
+    err = np.abs(out - ref).max() / np.abs(ref).max()
+    assert err < tol, (G, err)
+
+
+def test_exact_slice_accumulation_is_exact():
+    # entries k/64 (|k| <= 64): one or two 6-bit slices hold them exactly, so
+    # the product must equal the exact integer result bit for bit, over a K
+    # long enough for many exact FP32 chunks (1024 products each) and a
+    # split of the k loop over CTAs
+    rng = np.random.default_rng(5)
+    M, N, K = 150, 140, 5000
+    Ai = rng.integers(-64, 65, size=(M, K))
+    Bi = rng.integers(-64, 65, size=(N, K))
+    Ai[3, :] = 64                      # a row at exactly 1.0: its scale is 2, two slices
+    Bi[7, :] = -64
+    A, B = Ai / 64.0, Bi / 64.0
+    rc, out = _run(3, "mk,nk->mn", A, B, np.zeros((M, N)))
+    assert rc == 0
+    ref = (Ai @ Bi.T).astype(np.float64) / 4096.0      # exact: |sum| < 2^53
+    assert np.array_equal(out, ref), np.abs(out - ref).max()
