@@ -70,58 +70,72 @@ struct ErrSlots {
 //   Tnew = T + dT, accumulate dT^2, store dT as the DIIS error (FP32 or FP64),
 //   accumulate dot(dT, e_k) with the other stored errors, and the energy
 //   contribution Lt * (Tnew + t1new_ia t1new_jb) (T2 only).
-// rank 2: index e -> (i, a); rank 4: e -> (i, j, a, b), b fastest.
+// rank 2: index e -> (i, a); rank 4: e -> (i, j, a, b), b fastest.  For T2
+// each warp takes whole rows (i, j, a) so the index arithmetic and
+// e_i + e_j - e_a are per row; lanes read consecutive pairs of b with 128-bit
+// loads (v even) or single elements.
+__device__ __forceinline__ void update_one(int64_t e, double t, double r, double D, double t1ab, const double* Lt,
+                                           float* err_s, double* err_d, const ErrSlots& others, double& tn,
+                                           double (&vals)[NPART]) {
+  const double dt = r / D;
+  tn = t + dt;
+  vals[0] += dt * dt;
+  if (Lt) vals[1] += Lt[e] * (tn + t1ab);
+  double ev;
+  if (err_s) { const float f = (float)dt; err_s[e] = f; ev = (double)f; }
+  else if (err_d) { err_d[e] = dt; ev = dt; }
+  else ev = dt;
+  for (int k = 0; k < others.n; ++k) vals[2 + k] += ev * (others.s[k] ? (double)others.s[k][e] : others.d[k][e]);
+}
+
 __global__ void __launch_bounds__(RED_THREADS) update_kernel(
     int rank, const double* __restrict__ T, const double* __restrict__ R, const double* __restrict__ eps,
     int o, int v, double* __restrict__ Tnew, float* __restrict__ err_s, double* __restrict__ err_d,
     ErrSlots others, const double* __restrict__ Lt, const double* __restrict__ t1new, double* part) {
-  const int64_t total = rank == 2 ? (int64_t)o * v : (int64_t)o * o * v * v;
   double vals[NPART];
 #pragma unroll
   for (int k = 0; k < NPART; ++k) vals[k] = 0.0;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  // two elements per step with 128-bit loads when the pair is aligned
-  for (int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 2; p < total; p += 2 * stride) {
-    double tv[2], rv[2];
-    int cnt = (p + 1 < total) ? 2 : 1;
-    if (cnt == 2 && ((reinterpret_cast<uintptr_t>(T + p) | reinterpret_cast<uintptr_t>(R + p)) & 15) == 0) {
-      double2 t2v = *reinterpret_cast<const double2*>(T + p);
-      double2 r2v = *reinterpret_cast<const double2*>(R + p);
-      tv[0] = t2v.x; tv[1] = t2v.y; rv[0] = r2v.x; rv[1] = r2v.y;
-    } else {
-      for (int q = 0; q < cnt; ++q) { tv[q] = T[p + q]; rv[q] = R[p + q]; }
+  if (rank == 2) {
+    const int total = o * v;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+      const int i = e / v, a = e - i * v;
+      double tn;
+      update_one(e, T[e], R[e], eps[i] - eps[o + a], 0.0, nullptr, err_s, err_d, others, tn, vals);
+      Tnew[e] = tn;
     }
-    double tn[2], dt[2];
-    for (int q = 0; q < cnt; ++q) {
-      int64_t e = p + q;
-      double D;
-      int64_t i, j = 0, a, b = 0;
-      if (rank == 2) {
-        i = e / v; a = e - i * v;
-        D = eps[i] - eps[o + a];
+  } else {
+    const int lane = threadIdx.x & 31;
+    const int64_t nrows = (int64_t)o * o * v;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const bool pairs = (v & 1) == 0;
+    for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nrows; row += nw) {
+      const int a = (int)(row % v);
+      const int64_t ij = row / v;
+      const int j = (int)(ij % o), i = (int)(ij / o);
+      const double Drow = eps[i] + eps[j] - eps[o + a];
+      const double t1ia = Lt ? t1new[(int64_t)i * v + a] : 0.0;
+      const double* t1j = t1new + (int64_t)j * v;
+      const double* ev = eps + o;
+      const int64_t base = row * v;
+      if (pairs) {
+        for (int b = 2 * lane; b < v; b += 64) {
+          const int64_t e = base + b;
+          const double2 tv = *reinterpret_cast<const double2*>(T + e);
+          const double2 rv = *reinterpret_cast<const double2*>(R + e);
+          double2 tn;
+          update_one(e, tv.x, rv.x, Drow - ev[b], Lt ? t1ia * t1j[b] : 0.0, Lt, err_s, err_d, others, tn.x, vals);
+          update_one(e + 1, tv.y, rv.y, Drow - ev[b + 1], Lt ? t1ia * t1j[b + 1] : 0.0, Lt, err_s, err_d, others,
+                     tn.y, vals);
+          *reinterpret_cast<double2*>(Tnew + e) = tn;
+        }
       } else {
-        b = e % v; int64_t r = e / v;
-        a = r % v; r /= v;
-        j = r % o; i = r / o;
-        D = eps[i] + eps[j] - eps[o + a] - eps[o + b];
+        for (int b = lane; b < v; b += 32) {
+          const int64_t e = base + b;
+          double tn;
+          update_one(e, T[e], R[e], Drow - ev[b], Lt ? t1ia * t1j[b] : 0.0, Lt, err_s, err_d, others, tn, vals);
+          Tnew[e] = tn;
+        }
       }
-      dt[q] = rv[q] / D;
-      tn[q] = tv[q] + dt[q];
-      vals[0] += dt[q] * dt[q];
-      if (rank == 4 && Lt) vals[1] += Lt[e] * (tn[q] + t1new[i * v + a] * t1new[j * v + b]);
-      double ev;
-      if (err_s) { float f = (float)dt[q]; err_s[e] = f; ev = (double)f; }
-      else if (err_d) { err_d[e] = dt[q]; ev = dt[q]; }
-      else ev = dt[q];
-      for (int k = 0; k < others.n; ++k) {
-        double oe = others.s[k] ? (double)others.s[k][e] : others.d[k][e];
-        vals[2 + k] += ev * oe;
-      }
-    }
-    if (cnt == 2 && (reinterpret_cast<uintptr_t>(Tnew + p) & 15) == 0) {
-      *reinterpret_cast<double2*>(Tnew + p) = make_double2(tn[0], tn[1]);
-    } else {
-      for (int q = 0; q < cnt; ++q) Tnew[p + q] = tn[q];
     }
   }
   block_reduce_store(vals, 2 + others.n, part);
@@ -154,42 +168,61 @@ __global__ void __launch_bounds__(RED_THREADS) extrapolate_kernel(int rank, int 
                                                                   double* __restrict__ out,
                                                                   const double* __restrict__ Lt,
                                                                   const double* __restrict__ t1new, double* part) {
-  const int64_t total = rank == 2 ? (int64_t)o * v : (int64_t)o * o * v * v;
   double vals[NPART];
 #pragma unroll
   for (int k = 0; k < NPART; ++k) vals[k] = 0.0;
   double c[MAX_DIIS];
   for (int k = 0; k < sl.n; ++k) c[k] = coef[k];
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+  auto combine = [&](int64_t e) {
     double s = 0.0;
     for (int k = 0; k < sl.n; ++k) {
-      double ev = sl.es[k] ? (double)sl.es[k][e] : sl.ed[k][e];
+      const double ev = sl.es[k] ? (double)sl.es[k][e] : sl.ed[k][e];
       s += c[k] * sl.vec[k][e] + c[k] * ev;
     }
     out[e] = s;
-    if (rank == 4 && Lt) {
-      int64_t b = e % v, r = e / v, a = r % v;
-      r /= v;
-      int64_t j = r % o, i = r / o;
-      vals[1] += Lt[e] * (s + t1new[i * v + a] * t1new[j * v + b]);
+    return s;
+  };
+  if (rank == 2) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < o * v; e += gridDim.x * blockDim.x) combine(e);
+  } else {
+    // whole rows (i, j, a) per warp, lanes along b
+    const int lane = threadIdx.x & 31;
+    const int64_t nrows = (int64_t)o * o * v;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nrows; row += nw) {
+      const int a = (int)(row % v);
+      const int64_t ij = row / v;
+      const int j = (int)(ij % o), i = (int)(ij / o);
+      const double t1ia = Lt ? t1new[(int64_t)i * v + a] : 0.0;
+      for (int b = lane; b < v; b += 32) {
+        const int64_t e = row * v + b;
+        const double s = combine(e);
+        if (Lt) vals[1] += Lt[e] * (s + t1ia * t1new[(int64_t)j * v + b]);
+      }
     }
   }
   block_reduce_store(vals, 2, part);
 }
 
-// Energy of given amplitudes: sum Lt * (t2 + t1 t1).
+// Energy of given amplitudes: sum Lt * (t2 + t1 t1), whole rows (i, j, a) per warp.
 __global__ void __launch_bounds__(RED_THREADS) energy_kernel(int o, int v, const double* __restrict__ t2,
                                                              const double* __restrict__ t1,
                                                              const double* __restrict__ Lt, double* part) {
-  const int64_t total = (int64_t)o * o * v * v;
   double vals[NPART];
 #pragma unroll
   for (int k = 0; k < NPART; ++k) vals[k] = 0.0;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    int64_t b = e % v, r = e / v, a = r % v;
-    r /= v;
-    int64_t j = r % o, i = r / o;
-    vals[1] += Lt[e] * (t2[e] + t1[i * v + a] * t1[j * v + b]);
+  const int lane = threadIdx.x & 31;
+  const int64_t nrows = (int64_t)o * o * v;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nrows; row += nw) {
+    const int a = (int)(row % v);
+    const int64_t ij = row / v;
+    const int j = (int)(ij % o), i = (int)(ij / o);
+    const double t1ia = t1[(int64_t)i * v + a];
+    for (int b = lane; b < v; b += 32) {
+      const int64_t e = row * v + b;
+      vals[1] += Lt[e] * (t2[e] + t1ia * t1[(int64_t)j * v + b]);
+    }
   }
   block_reduce_store(vals, 2, part);
 }
@@ -403,6 +436,7 @@ void setup_integrals(fcc_ctx* c) {
   c->P.alloc(o * o * v * v);
   c->Cint.alloc(o * o * v * v);
   c->Dint.alloc(o * o * v * v);
+  c->Fring.alloc(o * o * v * v);
   c->Xo.alloc(o * o * o * o);
   c->Xq.alloc(Q * o * v);
   c->Yq.alloc(Q * o * v);
@@ -564,8 +598,12 @@ void residual(fcc_ctx* c) {
   einsum1(-1.0, "kiac->aikc", Ci, 1.0, Di, s);                          // - (ac|ki)
   einsum(0.5, "ilad,ldkc->aikc", u, L, 1.0, Di, s);
   einsum(-0.5, "liad,kdlc->kiac", t2, ovov, 1.0, Ci, s);
-  einsum(-0.5, "kjbc,kiac->ijab", t2, Ci, 0.0, P, s);
-  einsum(-1.0, "kibc,kjac->ijab", t2, Ci, 1.0, P, s);
+  // -1/2 t_kj^bc C_ki^ac - t_ki^bc C_kj^ac = -1/2 F_ijab - F_jiab with
+  // F_ijab = t_kj^bc C_ki^ac: one o^3 v^3 contraction instead of two
+  TView Fr = rm(c->Fring.p, {o, o, v, v});
+  einsum(1.0, "kjbc,kiac->ijab", t2, Ci, 0.0, Fr, s);
+  einsum1(-0.5, "ijab->ijab", Fr, 0.0, P, s);
+  einsum1(-1.0, "jiab->ijab", Fr, 1.0, P, s);
   einsum(0.5, "jkbc,aikc->ijab", u, Di, 1.0, P, s);
   // Fock-like terms
   TView Fvvp = rm(c->Fvv.p, {v, v}), Foop = rm(c->Foo.p, {o, o});
@@ -625,6 +663,7 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
   c->tc.err = c->dev_err.p;
   double best_rms = 1e300;
   int stalled = 0;
+  int exact_groups = 0;   // exact-slice width of the last exact-slice iteration
   bool diis = op.diis != 0;
   bool fp32err = op.diis_prec != 64;
 
@@ -787,10 +826,16 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
       TcScope scope(kind == K_F64 ? nullptr : &c->tc);
       c->tc.enabled = kind != K_F64;
       c->tc.exact = kind == K_EXACT;
-      // exact-slice width: 6 weight groups (15 slice pairs, ~3e-9 of the
-      // largest terms) while the amplitudes still move by more than max_rms,
-      // 8 groups (28 pairs, ~1e-12) for the last iterations
-      c->tc.oz_groups = rms >= op.max_rms ? 6 : OZ_G_DEFAULT;
+      // exact-slice width: 7 weight groups (21 slice pairs; their noise floor
+      // in the Jacobi step is ~1e-10 at (H2O)8) while the step is above
+      // max_rms, then 8 groups (28 pairs) to the end.  (6 groups floor at
+      // ~1e-8.)  The width only grows, so the phase cannot cycle.
+      if (kind == K_EXACT) {
+        const int groups = (exact_groups == OZ_G_DEFAULT || rms < op.max_rms) ? OZ_G_DEFAULT : OZ_G_DEFAULT - 1;
+        if (groups != exact_groups) { best_rms = 1e300; stalled = 0; }
+        exact_groups = groups;
+        c->tc.oz_groups = groups;
+      }
       c->tc.scheme = SPLIT3;
       residual(c);                                                         // :190
     }
@@ -842,7 +887,7 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
         // change is the next step of the same convergence) meets them at once
         const bool tight = rms < 0.1 * op.max_rms && std::fabs(dE) < 0.1 * op.e_conv &&
                            std::fabs(prev_dE) < op.e_conv;
-        if (tight || stalled >= 3) kind = K_F64;
+        if (tight || stalled >= 5) kind = K_F64;
       }
     }
     FCC_CUDA(cudaEventRecord(ev1, s));

@@ -30,7 +30,7 @@ struct fcc_ctx {
   // amplitudes and residuals
   fcc::DBuf<double> t1, t2;   // current amplitudes [o][v], [o][o][v][v]
   fcc::DBuf<double> r1, r2;   // residuals
-  fcc::DBuf<double> u, P, Cint, Dint, Xo, Wslab, Xq, Yq, Fvv, Foo;
+  fcc::DBuf<double> u, P, Cint, Dint, Fring, Xo, Wslab, Xq, Yq, Fvv, Foo;
   // symmetric / antisymmetric pp-ladder: pair tables (int2), channels
   fcc::DBuf<int2> pairP_v, pairM_v, pairP_o, pairM_o;   // (x<=y) and (x<y) pairs, row-major
   fcc::DBuf<double> Tp, Tm, Wp, Wm, LXp, LXm;

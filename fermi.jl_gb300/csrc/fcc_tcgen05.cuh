@@ -79,5 +79,19 @@ __device__ __forceinline__ void tc_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
+// Output tile of linear block index lin on a tm x tn tile grid, walked in
+// groups of 8 tile rows (row fastest inside a group) so that the CTAs resident
+// at the same time share A and B panels in L2.
+__device__ __forceinline__ void grouped_tile(int64_t lin, int64_t tm, int64_t tn, int64_t& mt, int64_t& nt) {
+  constexpr int64_t GM = 8;
+  const int64_t per_group = GM * tn;
+  const int64_t g = lin / per_group;
+  const int64_t first = g * GM;
+  const int64_t gm = tm - first < GM ? tm - first : GM;
+  const int64_t r = lin - g * per_group;
+  mt = first + r % gm;
+  nt = r / gm;
+}
+
 }  // namespace tc5
 }  // namespace fcc

@@ -178,8 +178,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_holder;
-  const int64_t m0 = (int64_t)blockIdx.x * OZ_BM;
-  const int64_t n0 = (int64_t)blockIdx.y * OZ_BN;
+  int64_t mt, nt;
+  grouped_tile(blockIdx.x, (ep.M + OZ_BM - 1) / OZ_BM, (ep.N + OZ_BN - 1) / OZ_BN, mt, nt);
+  const int64_t m0 = mt * OZ_BM;
+  const int64_t n0 = nt * OZ_BN;
   const int total = pr.n * nkb;
   const int st0 = (int)blockIdx.z * steps_per_split;
   const int st1 = min(total, st0 + steps_per_split);
@@ -560,8 +562,8 @@ void gemm_oz(const __nv_bfloat16* A, int64_t a_rows, const int* exA, const __nv_
   EpiMap e2 = ep;
   e2.atomic = (splits > 1 || ep.beta != 0.0) ? 1 : 0;
   if (e2.atomic && ep.beta != 1.0) scale_output(ep, ep.beta, s);
-  dim3 grid((unsigned)tm, (unsigned)tn, (unsigned)splits);
-  if (grid.y > 65535 || grid.x > 2147483647u) fail(FCC_ERR_BAD_ARG, "exact-slice grid too large");
+  if (tm * tn > 2147483647ll) fail(FCC_ERR_BAD_ARG, "exact-slice grid too large");
+  dim3 grid((unsigned)(tm * tn), 1u, (unsigned)splits);
   const int pidx = prof_begin(s);
   gemm_oz_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(ta, tb, nkb, (int)Kpad, pr, per, exA, exB, G, e2, err);
   FCC_CHECK_LAUNCH();

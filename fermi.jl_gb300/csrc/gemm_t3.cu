@@ -39,18 +39,38 @@ struct T3Cfg {
   static constexpr int B_BYTES = BN * T3_BK * 2;
   static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024;
-  static constexpr int TMEM_COLS = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
+  static constexpr int TMEM_COLS = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;   // per accumulator (two)
 };
 
 __device__ __forceinline__ int t3_sel(int code, int i, int j, int k) { return code == 0 ? i : (code == 1 ? j : k); }
 
+// tile t -> (m-tile, group, k - k0), m-tile fastest
+struct T3Tile {
+  int mt, g, kq;
+};
+__device__ __forceinline__ T3Tile t3_tile(int t, int tm) {
+  T3Tile r;
+  r.mt = t % tm;
+  const int q = t / tm;
+  r.g = q % 3;
+  r.kq = q / 3;
+  return r;
+}
+
+// Persistent: each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ...;
+// the TMA thread streams the K segments of its tiles through a shared-memory
+// ring, the MMA thread alternates two TMEM accumulators, and the epilogue
+// warps store tile t while the MMAs of tile t+1 run.
 template <int BN>
-__global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_constant__ T3Params P) {
+__global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_constant__ T3Params P, int tm,
+                                                                 int ntiles) {
   using Cfg = T3Cfg<BN>;
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[Cfg::STAGES];
   __shared__ __align__(8) uint64_t empty_bar[Cfg::STAGES];
-  __shared__ __align__(8) uint64_t acc_bar;
+  __shared__ __align__(8) uint64_t accf_bar[2];   // accumulator b holds a finished tile
+  __shared__ __align__(8) uint64_t acce_bar[2];   // accumulator b has been read out
+  __shared__ __align__(8) uint64_t done_bar;      // every issued MMA has completed
   __shared__ uint32_t tmem_holder;
   __shared__ int abort_flag;
   __shared__ float epi_tile[4][32][33];
@@ -59,23 +79,24 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
   uint8_t* sA = smem;
   uint8_t* sB = smem + Cfg::STAGES * Cfg::A_BYTES;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = blockIdx.y;
-  const int kk = P.k0 + (int)blockIdx.z;
   const int64_t v = P.v, o = P.o;
-  const int64_t m0 = (int64_t)blockIdx.x * T3_BM;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < Cfg::STAGES; ++s) {
       mbar_init(smem_u32(&full_bar[s]), 1);
       mbar_init(smem_u32(&empty_bar[s]), 1);
     }
-    mbar_init(smem_u32(&acc_bar), 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&accf_bar[b]), 1);
+      mbar_init(smem_u32(&acce_bar[b]), 4);   // one arrival per epilogue warp
+    }
+    mbar_init(smem_u32(&done_bar), 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_holder)),
-                 "r"(Cfg::TMEM_COLS)
+                 "r"(2 * Cfg::TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -83,26 +104,29 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_holder;
-  int total = 0;
-  for (int s = 0; s < T3_NSEG; ++s) total += P.seg[g][s].nkb;
 
   if (warp == 0 && lane == 0) {
-    // ---------------- TMA producer over the four K segments
+    // ---------------- TMA producer over the tiles' K segments
     int it = 0;
     bool stop = false;
-    for (int s = 0; s < T3_NSEG && !stop; ++s) {
-      const T3Seg sg = P.seg[g][s];
-      const int32_t arow = (int32_t)(t3_sel(sg.asel, P.i, P.j, kk) * v * v + m0);
-      const int32_t brow = (int32_t)((t3_sel(sg.bsel1, P.i, P.j, kk) * o + t3_sel(sg.bsel2, P.i, P.j, kk)) * v);
-      for (int kb = 0; kb < sg.nkb; ++kb, ++it) {
-        const int st = it % Cfg::STAGES;
-        const uint32_t ph = (it / Cfg::STAGES) & 1;
-        if (!mbar_wait(smem_u32(&empty_bar[st]), ph ^ 1)) { atomicExch(&abort_flag, 1); stop = true; break; }
-        if (*(volatile int*)&abort_flag) { stop = true; break; }
-        const uint32_t fb = smem_u32(&full_bar[st]);
-        mbar_expect_tx(fb, Cfg::STAGE_BYTES);
-        tma_load_2d(smem_u32(sA + st * Cfg::A_BYTES), &P.maps[sg.amap], kb * T3_BK, arow, fb);
-        tma_load_2d(smem_u32(sB + st * Cfg::B_BYTES), &P.maps[sg.bmap], kb * T3_BK, brow, fb);
+    for (int t = blockIdx.x; t < ntiles && !stop; t += gridDim.x) {
+      const T3Tile tl = t3_tile(t, tm);
+      const int kk = P.k0 + tl.kq;
+      const int64_t m0 = (int64_t)tl.mt * T3_BM;
+      for (int s = 0; s < T3_NSEG && !stop; ++s) {
+        const T3Seg sg = P.seg[tl.g][s];
+        const int32_t arow = (int32_t)(t3_sel(sg.asel, P.i, P.j, kk) * v * v + m0);
+        const int32_t brow = (int32_t)((t3_sel(sg.bsel1, P.i, P.j, kk) * o + t3_sel(sg.bsel2, P.i, P.j, kk)) * v);
+        for (int kb = 0; kb < sg.nkb; ++kb, ++it) {
+          const int st = it % Cfg::STAGES;
+          const uint32_t ph = (it / Cfg::STAGES) & 1;
+          if (!mbar_wait(smem_u32(&empty_bar[st]), ph ^ 1)) { atomicExch(&abort_flag, 1); stop = true; break; }
+          if (*(volatile int*)&abort_flag) { stop = true; break; }
+          const uint32_t fb = smem_u32(&full_bar[st]);
+          mbar_expect_tx(fb, Cfg::STAGE_BYTES);
+          tma_load_2d(smem_u32(sA + st * Cfg::A_BYTES), &P.maps[sg.amap], kb * T3_BK, arow, fb);
+          tma_load_2d(smem_u32(sB + st * Cfg::B_BYTES), &P.maps[sg.bmap], kb * T3_BK, brow, fb);
+        }
       }
     }
     if (stop) {
@@ -113,42 +137,60 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer
     constexpr uint32_t idesc = idesc_bf16(T3_BM, BN);
-    for (int it = 0; it < total; ++it) {
-      const int st = it % Cfg::STAGES;
-      const uint32_t ph = (it / Cfg::STAGES) & 1;
-      if (!mbar_wait(smem_u32(&full_bar[st]), ph)) { atomicExch(&abort_flag, 1); break; }
+    int it = 0, lt = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++lt) {
+      const int g = t3_tile(t, tm).g;
+      int total = 0;
+      for (int s = 0; s < T3_NSEG; ++s) total += P.seg[g][s].nkb;
+      const int b = lt & 1;
+      if (!mbar_wait(smem_u32(&acce_bar[b]), ((lt >> 1) & 1) ^ 1)) { atomicExch(&abort_flag, 1); break; }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint64_t ad = sw128_desc(smem_u32(sA + st * Cfg::A_BYTES));
-      const uint64_t bd = sw128_desc(smem_u32(sB + st * Cfg::B_BYTES));
+      const uint32_t dcol = tmem + (uint32_t)(b * Cfg::TMEM_COLS);
+      for (int x = 0; x < total; ++x, ++it) {
+        const int st = it % Cfg::STAGES;
+        const uint32_t ph = (it / Cfg::STAGES) & 1;
+        if (!mbar_wait(smem_u32(&full_bar[st]), ph)) { atomicExch(&abort_flag, 1); ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint64_t ad = sw128_desc(smem_u32(sA + st * Cfg::A_BYTES));
+        const uint64_t bd = sw128_desc(smem_u32(sB + st * Cfg::B_BYTES));
 #pragma unroll
-      for (int q = 0; q < T3_BK / 16; ++q) {
-        const uint32_t acc = (it > 0 || q > 0) ? 1u : 0u;
-        asm volatile(
-            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-            "l"(ad + (uint64_t)(2 * q)), "l"(bd + (uint64_t)(2 * q)), "r"(idesc), "r"(acc)
-            : "memory");
+        for (int q = 0; q < T3_BK / 16; ++q) {
+          const uint32_t acc = (x > 0 || q > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dcol),
+              "l"(ad + (uint64_t)(2 * q)), "l"(bd + (uint64_t)(2 * q)), "r"(idesc), "r"(acc)
+              : "memory");
+        }
+        tc_commit(smem_u32(&empty_bar[st]));
       }
-      tc_commit(smem_u32(&empty_bar[st]));
+      if (!ok) break;
+      tc_commit(smem_u32(&accf_bar[b]));
     }
-    tc_commit(smem_u32(&acc_bar));
+    // TMEM is freed only after every issued MMA has completed (also on an abort)
+    tc_commit(smem_u32(&done_bar));
+    if (!mbar_wait(smem_u32(&done_bar), 0)) atomicExch(&abort_flag, 1);
   } else if (warp >= 2) {
     // ---------------- epilogue: TMEM -> transposed 32 x 32 blocks -> plain FP32 stores
-    bool ok = mbar_wait(smem_u32(&acc_bar), 0);
-    ok = __all_sync(0xffffffffu, ok);
-    if (!ok) atomicExch(&abort_flag, 1);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int q = warp & 3;
-    const bool abort_now = __any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0);
-    if (ok && !abort_now) {
-      const int64_t v2 = v * v;
-      float* out = P.G + ((int64_t)g * P.nk + blockIdx.z) * v2 * v;
-      float (*tile)[33] = epi_tile[q];
+    const int64_t v2 = v * v;
+    float (*tile)[33] = epi_tile[q];
+    int lt = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+      const T3Tile tl = t3_tile(t, tm);
+      const int b = lt & 1;
+      bool ok = mbar_wait(smem_u32(&accf_bar[b]), (lt >> 1) & 1);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok || __any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0)) { atomicExch(&abort_flag, 1); break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int64_t m0 = (int64_t)tl.mt * T3_BM;
+      float* out = P.G + ((int64_t)tl.g * P.nk + tl.kq) * v2 * v;
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 32) {
         if (c0 >= v) break;
         uint32_t r[32];
-        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * Cfg::TMEM_COLS + c0);
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -171,13 +213,18 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
           }
         }
       }
+      // the accumulator is free for the tile after next
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&acce_bar[b]));
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cfg::TMEM_COLS) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * Cfg::TMEM_COLS)
+                 : "memory");
   }
   if (threadIdx.x == 0 && abort_flag) atomicExch(P.err, 1);
 }
@@ -190,8 +237,10 @@ void launch_t3(const T3Params& P, cudaStream_t s) {
     cudaFuncSetAttribute(gemm_t3_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM);
   });
   const int64_t tm = ((int64_t)P.v * P.v + T3_BM - 1) / T3_BM;
-  dim3 grid((unsigned)tm, 3u, (unsigned)P.nk);
-  gemm_t3_kernel<BN><<<grid, T3_THREADS, Cfg::SMEM, s>>>(P);
+  const int64_t ntiles = tm * 3 * P.nk;
+  if (ntiles > (int64_t)1 << 30) fail(FCC_ERR_BAD_ARG, "too many (T) tiles in one launch");
+  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, 152);
+  gemm_t3_kernel<BN><<<grid, T3_THREADS, Cfg::SMEM, s>>>(P, (int)tm, (int)ntiles);
   FCC_CHECK_LAUNCH();
 }
 

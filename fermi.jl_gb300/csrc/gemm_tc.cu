@@ -86,8 +86,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_holder;
-  const int64_t m0 = (int64_t)blockIdx.x * BM;
-  const int64_t n0 = (int64_t)blockIdx.y * BN;
+  int64_t mt, nt;
+  grouped_tile(blockIdx.x, (ep.M + BM - 1) / BM, (ep.N + BN - 1) / BN, mt, nt);
+  const int64_t m0 = mt * BM;
+  const int64_t n0 = nt * BN;
   // split-K: this CTA reduces k-tiles [kb, ke); partial sums are added atomically
   const int kb = (int)blockIdx.z * k_chunk;
   const int ke = min(num_k, kb + k_chunk);
@@ -407,8 +409,8 @@ void launch_tc(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __n
     FCC_CHECK_LAUNCH();
     e2.atomic = 1;
   }
-  dim3 grid((unsigned)tm, (unsigned)tn, (unsigned)splits);
-  if (grid.y > 65535) fail(FCC_ERR_BAD_ARG, "tensor-core grid too large");
+  if (tm * tn > 2147483647ll) fail(FCC_ERR_BAD_ARG, "tensor-core grid too large");
+  dim3 grid((unsigned)(tm * tn), 1u, (unsigned)splits);
   const int pidx = prof_begin(s);
   gemm_bf16_tc_kernel<BN><<<grid, TC_THREADS, Cfg::SMEM, s>>>(ta, tb, a_row0, b_row0, num_k, chunk, e2, err);
   FCC_CHECK_LAUNCH();

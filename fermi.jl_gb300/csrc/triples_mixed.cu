@@ -67,39 +67,41 @@ __global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
   auto role = [](int p, int r) { return (int)((PRC >> (8 * p + 2 * r)) & 3); };
   const int t = threadIdx.x;
 
-  // ---- stage W = G0[x][y][z] + G1[x][z][y] + G2[y][z][x] in three passes,
-  // each with its thread order along the source's stride-1 index
-  for (int e = t; e < 6 * ET * ET * ET; e += ETH) {
-    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
-    const int x = r / (ET * ET), y = (r / ET) % ET, z = r % ET;   // z fastest
-    const int X = org(role(p, 0)) + x, Y = org(role(p, 1)) + y, Z = org(role(p, 2)) + z;
-    Wt[p][x][y][z] = (X < v && Y < v && Z < v) ? G0[((int64_t)X * v + Y) * v + Z] : 0.0f;
-  }
-  __syncthreads();
-  for (int e = t; e < 6 * ET * ET * ET; e += ETH) {
-    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
-    const int x = r / (ET * ET), z = (r / ET) % ET, y = r % ET;   // y fastest
-    const int X = org(role(p, 0)) + x, Y = org(role(p, 1)) + y, Z = org(role(p, 2)) + z;
-    if (X < v && Y < v && Z < v) Wt[p][x][y][z] += G1[((int64_t)X * v + Z) * v + Y];
-  }
-  __syncthreads();
-  for (int e = t; e < 6 * ET * ET * ET; e += ETH) {
-    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
-    const int y = r / (ET * ET), z = (r / ET) % ET, x = r % ET;   // x fastest
-    const int X = org(role(p, 0)) + x, Y = org(role(p, 1)) + y, Z = org(role(p, 2)) + z;
-    if (X < v && Y < v && Z < v) Wt[p][x][y][z] += G2[((int64_t)Y * v + Z) * v + X];
-  }
-  // ---- (i y|j z)-type integrals and t1 on the blocks
+  // ---- stage W = G0[x][y][z] + G1[x][z][y] + G2[y][z][x] and the
+  // integral blocks: every thread first issues all its global loads (each
+  // source read along its stride-1 index), then writes shared memory, so one
+  // global latency covers the whole staging
+  constexpr int NE = 6 * ET * ET * ET / ETH;          // elements per thread per source
+  constexpr int NM = (9 * ET * ET + ETH - 1) / ETH;    // integral elements per thread
+  float g0[NE], g1[NE], g2[NE], mjk[NM], mik[NM], mij[NM];
   const int64_t mstr = (int64_t)o * v;
-  for (int e = t; e < 9 * ET * ET; e += ETH) {
-    const int rr = e / (ET * ET), q = e % (ET * ET);
-    const int r1 = rr / 3, r2 = rr % 3, y = q / ET, z = q % ET;
-    const int Y = org(r1) + y, Z = org(r2) + z;
-    const bool in = Y < v && Z < v;
-    // ovovf[p][y][q][z] = (p y|q z), row stride o*v
-    Mjk[r1][r2][y][z] = in ? ovovf[((int64_t)j * v + Y) * mstr + (int64_t)k * v + Z] : 0.0f;
-    Mik[r1][r2][y][z] = in ? ovovf[((int64_t)i * v + Y) * mstr + (int64_t)k * v + Z] : 0.0f;
-    Mij[r1][r2][y][z] = in ? ovovf[((int64_t)i * v + Y) * mstr + (int64_t)j * v + Z] : 0.0f;
+#pragma unroll
+  for (int q = 0; q < NE; ++q) {
+    const int e = t + q * ETH;
+    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
+    const int hi = r / (ET * ET), mid = (r / ET) % ET, lo = r % ET;
+    const int o0 = org(role(p, 0)), o1 = org(role(p, 1)), o2 = org(role(p, 2));
+    // G0[x][y][z], z fastest: (x, y, z) = (hi, mid, lo)
+    g0[q] = (o0 + hi < v && o1 + mid < v && o2 + lo < v) ? G0[((int64_t)(o0 + hi) * v + o1 + mid) * v + o2 + lo] : 0.0f;
+    // G1[x][z][y], y fastest: (x, z, y) = (hi, mid, lo)
+    g1[q] = (o0 + hi < v && o1 + lo < v && o2 + mid < v) ? G1[((int64_t)(o0 + hi) * v + o2 + mid) * v + o1 + lo] : 0.0f;
+    // G2[y][z][x], x fastest: (y, z, x) = (hi, mid, lo)
+    g2[q] = (o0 + lo < v && o1 + hi < v && o2 + mid < v) ? G2[((int64_t)(o1 + hi) * v + o2 + mid) * v + o0 + lo] : 0.0f;
+  }
+#pragma unroll
+  for (int q = 0; q < NM; ++q) {
+    const int e = t + q * ETH;
+    mjk[q] = mik[q] = mij[q] = 0.0f;
+    if (e < 9 * ET * ET) {
+      const int rr = e / (ET * ET), qq = e % (ET * ET);
+      const int Y = org(rr / 3) + qq / ET, Z = org(rr % 3) + qq % ET;
+      if (Y < v && Z < v) {
+        // ovovf[p][y][q][z] = (p y|q z), row stride o*v
+        mjk[q] = ovovf[((int64_t)j * v + Y) * mstr + (int64_t)k * v + Z];
+        mik[q] = ovovf[((int64_t)i * v + Y) * mstr + (int64_t)k * v + Z];
+        mij[q] = ovovf[((int64_t)i * v + Y) * mstr + (int64_t)j * v + Z];
+      }
+    }
   }
   if (t < 3 * ET) {
     const int r = t / ET, x = t % ET, X = org(r) + x;
@@ -108,8 +110,37 @@ __global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
     T1[2][r][x] = X < v ? t1f[(int64_t)k * v + X] : 0.0f;
     epsv[r][x] = X < v ? eps[o + X] : 0.0;
   }
+#pragma unroll
+  for (int q = 0; q < NM; ++q) {
+    const int e = t + q * ETH;
+    if (e < 9 * ET * ET) {
+      const int rr = e / (ET * ET), qq = e % (ET * ET);
+      Mjk[rr / 3][rr % 3][qq / ET][qq % ET] = mjk[q];
+      Mik[rr / 3][rr % 3][qq / ET][qq % ET] = mik[q];
+      Mij[rr / 3][rr % 3][qq / ET][qq % ET] = mij[q];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NE; ++q) {
+    const int e = t + q * ETH;
+    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
+    Wt[p][r / (ET * ET)][(r / ET) % ET][r % ET] = g0[q];
+  }
   __syncthreads();
-  if (t < ET * ET) Dab[t / ET][t % ET] = eps[i] + eps[j] + eps[k] - epsv[0][t / ET] - epsv[1][t % ET];
+#pragma unroll
+  for (int q = 0; q < NE; ++q) {
+    const int e = t + q * ETH;
+    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
+    Wt[p][r / (ET * ET)][r % ET][(r / ET) % ET] += g1[q];   // (x, z, y) order
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NE; ++q) {
+    const int e = t + q * ETH;
+    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
+    Wt[p][r % ET][r / (ET * ET)][(r / ET) % ET] += g2[q];   // (y, z, x) order
+  }
+  if (t < ET * ET) Dab[t / ET][t % ET] = eps[i] + eps[j] + eps[k] - eps[o + oa + t / ET] - eps[o + ob + t % ET];
   __syncthreads();
 
   // V(x,y,z) for x in block rx at lx etc.: W + t1_ix (jy|kz) + (ix|kz) t1_jy + (ix|jy) t1_kz
@@ -117,7 +148,7 @@ __global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
     return w + T1[0][rx][lx] * Mjk[ry][rz][ly][lz] + Mik[rx][rz][lx][lz] * T1[1][ry][ly] +
            Mij[rx][ry][lx][ly] * T1[2][rz][lz];
   };
-  double acc = 0.0;
+  float accf = 0.0f;   // two (a,b,c) per thread; the reductions over threads and blocks are FP64
   for (int e = t; e < ET * ET * ET; e += ETH) {
     const int la = e / (ET * ET), lb = (e / ET) % ET, lc = e % ET;
     const int a = oa + la, b = ob + lb, c = oc + lc;
@@ -135,8 +166,9 @@ __global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
     // is 1/64 rate: an FP64 division per (a,b,c) bounded this kernel)
     const double D = Dab[la][lb] - epsv[2][lc];
     const float wgt = 1.0f + (float)(a == b) + (float)(b == c);
-    acc += (double)__fdiv_rn(Ef, (float)D * wgt);
+    accf += __fdiv_rn(Ef, (float)D * wgt);
   }
+  double acc = (double)accf;
   for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
   if ((t & 31) == 0) red[t >> 5] = acc;
   __syncthreads();

@@ -12,6 +12,7 @@ guess; reports iterations to convergence, the converged energies and the
 guess errors.
 
     python -m fermicc.train_guess --n4 128 --n6 16 --steps 3000 --out params.f32
+    python -m fermicc.train_guess --eval-only --eval6 32 --eval8 4 --out eval
 """
 from __future__ import annotations
 
@@ -57,11 +58,13 @@ def build_training_set(model, n4, n6, seed0=0, stride4=8, stride6=32, log=print)
         log(f"(H2O){waters}: {count} seeds collected ({time.time() - t0:.1f} s)")
 
 
-def evaluate(model, cases, log=print):
+def evaluate(model, cases, log=print, precision="fp64"):
+    """Per held-out geometry: iterations from the MP2 and from the learned
+    guess (same criteria), the converged energies and the T2 guess errors."""
     out = []
     for waters, sd in cases:
         inp = scf.water_inputs(waters, seed=sd)
-        ref, ctx = solve(inp)
+        ref, ctx = solve(inp, precision=precision)
         T1c, T2c = ref.T1, ref.T2
         # guess quality: MP2 vs learned
         ctx.lib.fcc_set_guess(ctx.h, None, None)
@@ -71,7 +74,7 @@ def evaluate(model, cases, log=print):
         err_mp2 = float(np.sqrt(np.mean((T2mp2 - T2c) ** 2)))
         err_mlp = float(np.sqrt(np.mean((T2mlp - T2c) ** 2)))
         ctx.close()
-        lrn, ctx2 = solve(inp, guess_model=model)
+        lrn, ctx2 = solve(inp, guess_model=model, precision=precision)
         ctx2.close()
         row = dict(waters=waters, seed=sd, iters_mp2=len(ref.iterations), iters_mlp=len(lrn.iterations),
                    e_mp2=ref.energy, e_mlp=lrn.energy, de=abs(ref.energy - lrn.energy),
@@ -91,7 +94,22 @@ def main():
     ap.add_argument("--out", default="mlp_t2_guess.f32")
     ap.add_argument("--eval6", type=int, default=4)
     ap.add_argument("--eval8", type=int, default=2)
+    ap.add_argument("--eval-only", action="store_true",
+                    help="evaluate the packaged network (fermicc/data) instead of training one")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     a = ap.parse_args()
+    cases = [(6, 1000 + k) for k in range(a.eval6)] + [(8, 1000 + k) for k in range(a.eval8)]
+    if a.eval_only:
+        from .mlp import DEFAULT_PARAMS
+        rows = evaluate(MLPGuess(0, DEFAULT_PARAMS), cases, precision=a.precision)
+        summary = {k: float(np.mean([r[k] for r in rows])) for k in ("iters_mp2", "iters_mlp", "de",
+                                                                      "guess_rms_err_mp2", "guess_rms_err_mlp")}
+        summary["max_de"] = float(max(r["de"] for r in rows))
+        summary["cases"] = len(rows)
+        print(json.dumps({"summary": summary}), flush=True)
+        with open(a.out + ".eval.json", "w") as f:
+            json.dump({"precision": a.precision, "rows": rows, "summary": summary}, f, indent=1)
+        return
     model = MLPGuess(0)
     build_training_set(model, a.n4, a.n6)
     t = time.time()
@@ -100,7 +118,6 @@ def main():
           f"{np.mean(loss[-50:]):.4e}", flush=True)
     model.save(a.out)
     np.savetxt(a.out + ".loss.txt", loss)
-    cases = [(6, 1000 + k) for k in range(a.eval6)] + [(8, 1000 + k) for k in range(a.eval8)]
     rows = evaluate(model, cases)
     with open(a.out + ".eval.json", "w") as f:
         json.dump(rows, f, indent=1)
