@@ -900,6 +900,8 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
       FCC_CUDA(cudaMemcpy(&herr, c->dev_err.p, sizeof(int), cudaMemcpyDeviceToHost));
       if (herr) { status = FCC_ERR_TIMEOUT; }
     }
+    if (c->ckpt_every > 0 && ite % c->ckpt_every == 0)
+      checkpoint_write(c, c->ckpt_path, cur1, cur2, Ecc, ite, 0);
     if (log && nlog < log_cap) {
       fcc_iter_stats& L = log[nlog];
       L.ite = ite; L.diis = did; L.precision = iter_kind; L.pad = 0;
@@ -926,6 +928,10 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
     res->converged = conv_final ? 1 : 0;                                   // :231
   }
   c->have_ccsd = true;
+  c->last_ecc = Ecc;
+  c->last_iters = nlog;
+  c->last_converged = conv_final ? 1 : 0;
+  if (c->ckpt_every > 0) checkpoint_write(c, c->ckpt_path, c->t1.p, c->t2.p, Ecc, nlog, conv_final ? 1 : 0);
   return status;
 }
 

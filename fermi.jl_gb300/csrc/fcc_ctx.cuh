@@ -48,6 +48,11 @@ struct fcc_ctx {
   fcc::DBuf<int> dev_err;
   // statistics of the last run
   int64_t launches = 0;
+  double last_ecc = 0.0;      // correlation energy of the current amplitudes
+  int32_t last_iters = 0, last_converged = 0;
+  // periodic checkpoint of fcc_ccsd_run (empty path: off)
+  std::string ckpt_path;
+  int32_t ckpt_every = 0;
 
   // (T) scratch
   fcc::DBuf<double> ovvv, ooov, Wt;
@@ -61,4 +66,7 @@ void residual(fcc_ctx* c);
 int ccsd_run(fcc_ctx* c, const fcc_opts* opts, fcc_iter_stats* log, int32_t log_cap, fcc_ccsd_result* out);
 double triples_fp64(fcc_ctx* c);
 double triples_mixed(fcc_ctx* c);
+// write amplitudes (device, row-major) to a checkpoint file (checkpoint.cu)
+void checkpoint_write(fcc_ctx* c, const std::string& path, const double* t1, const double* t2, double ecc,
+                      int32_t iterations, int32_t converged);
 }  // namespace fcc

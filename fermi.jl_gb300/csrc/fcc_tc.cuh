@@ -74,8 +74,8 @@ void scale_output(const EpiMap& ep, double beta, cudaStream_t s);
 // cut into S = G-1 signed 6-bit digit slices, x = 2^e_r sum_s d_s 2^(-6(s+1)),
 // |d| <= 64, stored exactly in BF16.  A.B^T is the sum over slice pairs
 // (s, t) with s + t + 2 <= G of the digit products; pairs of one weight
-// 2^(-6(s+t+2)) are summed on the tensor cores in FP32 over chunks of 1024
-// products (|sum| < 2^22, so every partial sum is an exact integer) and the
+// 2^(-6(s+t+2)) are summed on the tensor cores in FP32 over chunks of 2048
+// products (|sum| <= 2^23, so every partial sum is an exact integer) and the
 // chunks are added in double-FP32 (~2^-48 relative) in TMEM.  The result
 // carries the slice truncation error, ~2^(-6(G-1)) of max|A_r| max|B_c| per
 // term (G = 8: ~1e-12 of max|C| for Gaussian operands).

@@ -3,9 +3,9 @@
 // C = alpha * A.B^T + beta * C for FP64 operands, evaluated from signed 6-bit
 // digit slices of A and B (see fcc_tc.cuh).  Every digit is an integer
 // |d| <= 64, exact in BF16; every product of two digits is an integer of at
-// most 2^12, so a run of 1024 products accumulated by tcgen05.mma in FP32
-// stays an exact integer (< 2^22).  The kernel therefore closes an
-// accumulation chunk every 16 k-blocks (or at the end of a weight group), and
+// most 2^12, so a run of 2048 products accumulated by tcgen05.mma in FP32
+// stays an exact integer (|sum| <= 2^23).  The kernel therefore closes an
+// accumulation chunk every 32 k-blocks (or at the end of a weight group), and
 // the epilogue warps add the chunk, times its weight 2^(-6g) (exact), into a
 // double-FP32 (hi + lo, ~2^-48 relative) running sum held in TMEM.  Two TMEM
 // accumulators alternate, so the MMA thread fills one while the epilogue
@@ -34,10 +34,10 @@ using namespace tc5;
 constexpr int OZ_BM = 128;
 constexpr int OZ_BN = 128;
 constexpr int OZ_BK = 64;
-constexpr int OZ_STAGES = 5;
+constexpr int OZ_STAGES = 7;
 constexpr int OZ_THREADS = 192;      // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int OZ_BITS = 6;           // bits per digit slice
-constexpr int OZ_CH = 16;            // k-blocks per exact FP32 chunk (16 * 64 = 1024 products)
+constexpr int OZ_CH = 32;            // k-blocks per exact FP32 chunk: 2048 products of at most 64*64, |sum| <= 2^23
 constexpr int OZ_MAXPAIRS = 40;
 constexpr int OZ_A_BYTES = OZ_BM * OZ_BK * 2;
 constexpr int OZ_B_BYTES = OZ_BN * OZ_BK * 2;
@@ -148,7 +148,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __shared__ __align__(8) uint64_t done_bar;      // every issued MMA has completed
   __shared__ uint32_t tmem_holder;
   __shared__ int abort_flag;
-  __shared__ double otile[4][32][33];             // per epilogue warp: 32 x 32 transpose
 
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* sA = smem;
@@ -308,7 +307,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       const bool apow2 = (ab & ((1ull << 52) - 1)) == 0 && ((ab >> 52) & 0x7FF) != 0;
       const int ka = apow2 ? (int)((ab >> 52) & 0x7FF) - 1023 : 0;
       const bool aneg = apow2 && (ab >> 63);
-      double (*tile)[33] = otile[q];
+      // per epilogue warp a 32 x 32 FP64 transpose tile, in the operand ring
+      // (every load has been consumed once done_bar has completed)
+      double (*tile)[33] = reinterpret_cast<double (*)[32][33]>(smem)[q];
 #pragma unroll 1
       for (int c0 = 0; c0 < OZ_BN; c0 += 32) {
         if (n0 + c0 >= ep.N) break;

@@ -15,6 +15,8 @@ keys the coupled-cluster path reads, plus the keys this backend adds:
 * ``cc_gpu_switch_rms`` -- residual at which the mixed form switches to FP64.
 * ``cc_gpu_guess`` -- "mp2" or "mlp" (learned T2 initialiser).
 * ``pt_gpu_precision`` -- "fp64" or "mixed" for (T).
+* ``cc_gpu_checkpoint`` / ``cc_gpu_checkpoint_every`` -- checkpoint file of the
+  amplitudes, written every N iterations and at the end of a run (0: off).
 """
 from __future__ import annotations
 
@@ -45,6 +47,8 @@ DEFAULT = {
     "cc_gpu_guess": "mp2",
     "pt_gpu_precision": "fp64",
     "cc_gpu_device": 0,
+    "cc_gpu_checkpoint": "",
+    "cc_gpu_checkpoint_every": 0,
 }
 
 _current: dict = {}

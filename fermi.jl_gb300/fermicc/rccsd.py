@@ -117,6 +117,19 @@ class Context:
         _check(self.lib, self.h, self.lib.fcc_get_amps(self.h, _ptr(T1), _ptr(T2)), "fcc_get_amps")
         return np.ascontiguousarray(T1), np.ascontiguousarray(T2)
 
+    def save_checkpoint(self, path: str):
+        """Write the current amplitudes (header + column-major T1, T2)."""
+        _check(self.lib, self.h, self.lib.fcc_checkpoint_save(self.h, str(path).encode()), "fcc_checkpoint_save")
+
+    def load_checkpoint(self, path: str):
+        """Make the amplitudes of a checkpoint the starting point of the next run."""
+        _check(self.lib, self.h, self.lib.fcc_checkpoint_load(self.h, str(path).encode()), "fcc_checkpoint_load")
+
+    def set_checkpoint(self, path: str | None, every: int):
+        """Checkpoint every `every` iterations of the next runs and at their end (0: off)."""
+        p = str(path).encode() if path else None
+        _check(self.lib, self.h, self.lib.fcc_set_checkpoint(self.h, p, int(every)), "fcc_set_checkpoint")
+
     def triples(self, precision: int) -> float:
         et = ctypes.c_double()
         _check(self.lib, self.h, self.lib.fcc_triples(self.h, precision, ctypes.byref(et)), "fcc_triples")
@@ -192,6 +205,11 @@ class RCCSD:
             model.guess(ctx)
         elif Options.get("cc_gpu_guess") != "mp2":
             raise FermiException(f"cc_gpu_guess must be mp2 or mlp, got {Options.get('cc_gpu_guess')!r}")
+        every = int(Options.get("cc_gpu_checkpoint_every"))
+        path = Options.get("cc_gpu_checkpoint")
+        if every < 0 or (every > 0 and not path):
+            raise FermiException("cc_gpu_checkpoint_every > 0 needs a cc_gpu_checkpoint path")
+        ctx.set_checkpoint(path if every > 0 else None, every)
         rc, res, lines = ctx.run(_opts_from_options())
         T1, T2 = ctx.amplitudes()
         return cls(res.guessenergy, res.correlation, res.energy, T1, T2, res.e_conv, res.t_conv,

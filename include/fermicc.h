@@ -133,6 +133,23 @@ int fcc_get_amps(fcc_ctx* ctx, double* T1, double* T2);
  * FCC_PREC_MIXED); et_out receives E(T). */
 int fcc_triples(fcc_ctx* ctx, int32_t precision, double* et_out);
 
+/* ---- checkpoints ----------------------------------------------------------
+ * Not in Fermi.jl, which restarts only through the guess arguments of
+ * RCCSD(moints, T1guess, T2guess, alg) (RCCSDa.jl:92).  A checkpoint file is
+ * a 64-byte header ("FCCCKPT1", version 1, o, v, naux as int32; correlation
+ * and reference energy as double; iterations done and converged as int32;
+ * 16 reserved bytes) followed by T1 (o x v) and T2 (o x o x v x v) in FP64,
+ * column-major, little-endian.  Writes go to path + ".tmp" and are renamed
+ * into place. */
+/* write the current amplitudes */
+int fcc_checkpoint_save(fcc_ctx* ctx, const char* path);
+/* read a checkpoint of the same (o, v) as the starting amplitudes of the
+ * next fcc_ccsd_run (as fcc_set_guess) */
+int fcc_checkpoint_load(fcc_ctx* ctx, const char* path);
+/* fcc_ccsd_run writes a checkpoint every `every` iterations and at its end
+ * (every = 0: off) */
+int fcc_set_checkpoint(fcc_ctx* ctx, const char* path, int32_t every);
+
 /* ---- learned T2 initialiser ---------------------------------------------
  * A 16 -> 128 -> 128 -> 1 GELU MLP predicting the CCSD correction to each
  * MP2 doubles amplitude from per-element features; BF16 weights with FP32

@@ -104,7 +104,7 @@ def test_exact_slice_groups_set_the_accuracy(G, tol):
 def test_exact_slice_accumulation_is_exact():
     # entries k/64 (|k| <= 64): one or two 6-bit slices hold them exactly, so
     # the product must equal the exact integer result bit for bit, over a K
-    # long enough for many exact FP32 chunks (1024 products each) and a
+    # long enough for several exact FP32 chunks (2048 products each) and a
     # split of the k loop over CTAs
     rng = np.random.default_rng(5)
     M, N, K = 150, 140, 5000
@@ -117,3 +117,14 @@ def test_exact_slice_accumulation_is_exact():
     assert rc == 0
     ref = (Ai @ Bi.T).astype(np.float64) / 4096.0      # exact: |sum| < 2^53
     assert np.array_equal(out, ref), np.abs(out - ref).max()
+
+
+def test_exact_slice_largest_chunk_sums_stay_exact():
+    # rows of 63/64 (one digit 63 each): every digit product is 3969, the
+    # largest a chunk of 2048 products can hold is ~2^23 -- still exact in FP32
+    M, N, K = 128, 128, 4100
+    A = np.full((M, K), 63.0 / 64.0)
+    B = np.full((N, K), -63.0 / 64.0)
+    rc, out = _run(3, "mk,nk->mn", A, B, np.zeros((M, N)))
+    assert rc == 0
+    assert np.array_equal(out, np.full((M, N), -K * 3969.0 / 4096.0))
