@@ -227,6 +227,32 @@ __global__ void __launch_bounds__(RED_THREADS) energy_kernel(int o, int v, const
   block_reduce_store(vals, 2, part);
 }
 
+// DF-MP2 correlation energy from (ia|jb) (RMP2a.jl:91-140 forms the same sum
+// pair by pair from the factors): sum (ia|jb) [2 (ia|jb) - (ib|ja)] / D_ijab,
+// whole rows (i, j, a) per warp, lanes along b.
+__global__ void __launch_bounds__(RED_THREADS) mp2_energy_kernel(int o, int v, const double* __restrict__ ovov,
+                                                                 const double* __restrict__ eps, double* part) {
+  double vals[NPART];
+#pragma unroll
+  for (int k = 0; k < NPART; ++k) vals[k] = 0.0;
+  const int lane = threadIdx.x & 31;
+  const int64_t nrows = (int64_t)o * o * v;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < nrows; row += nw) {
+    const int a = (int)(row % v);
+    const int64_t ij = row / v;
+    const int j = (int)(ij % o), i = (int)(ij / o);
+    const double Dia = eps[i] + eps[j] - eps[o + a];
+    const double* iajb = ovov + (((int64_t)i * v + a) * o + j) * v;   // (ia|jb) over b
+    for (int b = lane; b < v; b += 32) {
+      const double x = iajb[b];
+      const double y = ovov[(((int64_t)i * v + b) * o + j) * v + a];   // (ib|ja)
+      vals[1] += x * (2.0 * x - y) / (Dia - eps[o + b]);
+    }
+  }
+  block_reduce_store(vals, 2, part);
+}
+
 // Solve the bordered DIIS system B c = (0,..,0,1) in FP64 with partial
 // pivoting (DIIS.jl:66-87); one thread, N <= MAX_DIIS + 1.
 __global__ void diis_solve_kernel(const double* Bm, int N, double* coef, int* status) {
@@ -483,6 +509,19 @@ void make_mp2_guess(fcc_ctx* c) {
 double cc_energy(fcc_ctx* c, const double* t1, const double* t2) {
   cudaStream_t s = c->stream;
   energy_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>((int)c->o, (int)c->v, t2, t1, c->Lt.p, c->red.p);
+  FCC_CHECK_LAUNCH();
+  double* out = c->red.p + RED_BLOCKS * NPART;
+  finish_reduce_kernel<<<1, 32, 0, s>>>(c->red.p, RED_BLOCKS, 2, out);
+  FCC_CHECK_LAUNCH();
+  double h[2];
+  FCC_CUDA(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, s));
+  FCC_CUDA(cudaStreamSynchronize(s));
+  return h[1];
+}
+
+double mp2_energy(fcc_ctx* c) {
+  cudaStream_t s = c->stream;
+  mp2_energy_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>((int)c->o, (int)c->v, c->ovov.p, c->eps.p, c->red.p);
   FCC_CHECK_LAUNCH();
   double* out = c->red.p + RED_BLOCKS * NPART;
   finish_reduce_kernel<<<1, 32, 0, s>>>(c->red.p, RED_BLOCKS, 2, out);

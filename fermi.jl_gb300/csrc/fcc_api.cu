@@ -285,6 +285,16 @@ int fcc_get_amps(fcc_ctx* c, double* T1, double* T2) {
   });
 }
 
+int fcc_mp2_energy(fcc_ctx* c, double* e_corr) {
+  if (!c) return FCC_ERR_BAD_ARG;
+  return guarded(c, [&]() {
+    if (!e_corr) fcc::fail(FCC_ERR_BAD_ARG, "null output");
+    if (!c->have_ints) fcc::fail(FCC_ERR_STATE, "upload integrals first");
+    *e_corr = fcc::mp2_energy(c);
+    return std::isfinite(*e_corr) ? FCC_OK : FCC_ERR_NAN;
+  });
+}
+
 int fcc_triples(fcc_ctx* c, int32_t precision, double* et_out) {
   if (!c) return FCC_ERR_BAD_ARG;
   return guarded(c, [&]() {

@@ -62,6 +62,7 @@ namespace fcc {
 void setup_integrals(fcc_ctx* c);
 void make_mp2_guess(fcc_ctx* c);
 double cc_energy(fcc_ctx* c, const double* t1, const double* t2);
+double mp2_energy(fcc_ctx* c);
 void residual(fcc_ctx* c);
 int ccsd_run(fcc_ctx* c, const fcc_opts* opts, fcc_iter_stats* log, int32_t log_cap, fcc_ccsd_result* out);
 double triples_fp64(fcc_ctx* c);

@@ -7,7 +7,8 @@ Fermi's method objects and options, plus the stand-in input pipeline
 """
 from . import options as Options
 from .options import FermiException
-from .rccsd import CudaPT, RCCSD, RCCSDcuda, RCCSDpT, energy, get_pt_alg, get_rccsd_alg
+from .rccsd import (CudaPT, RCCSD, RCCSDcuda, RCCSDpT, RMP2, RMP2cuda, energy, get_pt_alg, get_rccsd_alg,
+                    get_rmp2_alg)
 
-__all__ = ["Options", "FermiException", "RCCSD", "RCCSDpT", "RCCSDcuda", "CudaPT", "energy",
-           "get_rccsd_alg", "get_pt_alg"]
+__all__ = ["Options", "FermiException", "RCCSD", "RCCSDpT", "RCCSDcuda", "CudaPT", "RMP2", "RMP2cuda", "energy",
+           "get_rccsd_alg", "get_pt_alg", "get_rmp2_alg"]

@@ -10,6 +10,8 @@ keys the coupled-cluster path reads, plus the keys this backend adds:
   ``RCCSDa`` and is not provided here.
 * ``pt_alg``  -- 4 selects this backend's (T) (``CudaPT``); Fermi's 1-3 are its
   Julia ``ijk`` / ``ijk2`` / ``abc``.
+* ``mp2_alg`` -- 3 selects this backend's DF-RMP2 energy (``RMP2cuda``); Fermi's
+  1-2 are its Julia ``RMP2a`` / ``RMP2b``.
 * ``cc_gpu_precision`` -- "fp64" or "mixed" (split-BF16 contractions with an
   FP64 finish).
 * ``cc_gpu_switch_rms`` -- residual at which the mixed form switches to FP64.
@@ -28,6 +30,7 @@ class FermiException(Exception):
 DEFAULT = {
     "cc_alg": 2,
     "pt_alg": 4,
+    "mp2_alg": 3,
     "cc_max_iter": 50,
     "cc_max_rms": 1e-10,
     "cc_e_conv": 1e-10,

@@ -12,7 +12,9 @@ types (``get_rccsd_alg(Val(N))``, src/Methods/CoupledCluster/RCCSD/RCCSD.jl:76-8
   boundary ``RCCSD(moints, T1guess, T2guess, alg)`` (RCCSDa.jl:92);
 * ``RCCSDpT.compute(ccsd, moints, alg=None)``: ``RCCSDpT(ccsd, moints, alg)``
   (ijk.jl:20);
-* ``energy("ccsd" | "ccsd(t)", moints)``: the ``@energy`` entry
+* ``RMP2.compute(moints)``: the DF-RMP2 energy (MollerPlesset/RMP2/RMP2a.jl:91-140)
+  from the same device integrals, ``mp2_alg = 3``;
+* ``energy("mp2" | "ccsd" | "ccsd(t)", moints)``: the ``@energy`` entry
   (src/Tools/SinglePointEnergy.jl:8-11,46).
 
 ``moints`` is a :class:`fermicc.inputs.scf.CCInputs` (the MO integral cache).
@@ -40,6 +42,18 @@ class RCCSDcuda:
 @dataclass(frozen=True)
 class CudaPT:
     """GB300 implementation of RCCSD(T) (``pt_alg = 4``)."""
+
+
+@dataclass(frozen=True)
+class RMP2cuda:
+    """GB300 implementation of the (DF-)RMP2 energy (``mp2_alg = 3``)."""
+
+
+def get_rmp2_alg(n: int | None = None):
+    n = Options.get("mp2_alg") if n is None else n
+    if n == 3:
+        return RMP2cuda()
+    raise FermiException(f"implementation number {n} not available for RMP2.")
 
 
 def get_rccsd_alg(n: int | None = None):
@@ -130,6 +144,12 @@ class Context:
         p = str(path).encode() if path else None
         _check(self.lib, self.h, self.lib.fcc_set_checkpoint(self.h, p, int(every)), "fcc_set_checkpoint")
 
+    def mp2_energy(self) -> float:
+        """MP2 correlation energy of the uploaded integrals (RMP2a.jl:91-140)."""
+        e = ctypes.c_double()
+        _check(self.lib, self.h, self.lib.fcc_mp2_energy(self.h, ctypes.byref(e)), "fcc_mp2_energy")
+        return e.value
+
     def triples(self, precision: int) -> float:
         et = ctypes.c_double()
         _check(self.lib, self.h, self.lib.fcc_triples(self.h, precision, ctypes.byref(et)), "fcc_triples")
@@ -169,6 +189,22 @@ def _opts_from_options() -> _lib.FccOpts:
     o.precision = _lib.FCC_PREC_FP64 if p == "fp64" else _lib.FCC_PREC_MIXED
     o.mixed_switch_rms = Options.get("cc_gpu_switch_rms")
     return o
+
+
+@dataclass
+class RMP2:
+    """Fields of Fermi's ``struct RMP2`` (MollerPlesset/RMP2/RMP2.jl:50-53)."""
+    correlation: float
+    energy: float
+
+    @classmethod
+    def compute(cls, moints, alg=None, context: Context | None = None) -> "RMP2":
+        alg = alg if alg is not None else get_rmp2_alg()
+        if not isinstance(alg, RMP2cuda):
+            raise FermiException(f"invalid arguments for RMP2 method: {type(alg).__name__}")
+        ctx = context or Context(moints)
+        e = ctx.mp2_energy()
+        return cls(e, e + moints.e_ref)
 
 
 @dataclass
@@ -240,6 +276,8 @@ class RCCSDpT:
 def energy(method: str, moints):
     """``@energy ccsd`` / ``@energy ccsd(t)`` on prepared MO integrals."""
     m = method.lower().replace(" ", "")
+    if m in ("mp2", "rmp2"):
+        return RMP2.compute(moints)
     if m in ("ccsd", "rccsd"):
         return RCCSD.compute(moints)
     if m in ("ccsd(t)", "rccsd(t)"):

@@ -133,6 +133,12 @@ int fcc_get_amps(fcc_ctx* ctx, double* T1, double* T2);
  * FCC_PREC_MIXED); et_out receives E(T). */
 int fcc_triples(fcc_ctx* ctx, int32_t precision, double* et_out);
 
+/* DF-MP2 (or conventional MP2) correlation energy of the uploaded integrals:
+ * sum_ijab (ia|jb) [2 (ia|jb) - (ib|ja)] / (e_i + e_j - e_a - e_b), the
+ * quantity RMP2_energy returns (MollerPlesset/RMP2/RMP2a.jl:91-140);
+ * RMP2.energy = e_corr + the reference energy. */
+int fcc_mp2_energy(fcc_ctx* ctx, double* e_corr);
+
 /* ---- checkpoints ----------------------------------------------------------
  * Not in Fermi.jl, which restarts only through the guess arguments of
  * RCCSD(moints, T1guess, T2guess, alg) (RCCSDa.jl:92).  A checkpoint file is

@@ -139,3 +139,16 @@ def test_diis_manager_semantics():
     dm.push(4 * np.ones(4), 0.2 * np.ones(4))
     assert len(dm) == 3
     assert all(float(e.max()) < 5 for e in dm.errs)
+
+
+def test_df_mp2_pair_loop_equals_the_mp2_guess_energy():
+    # RMP2a.jl's pair loop and the CC driver's MP2 guess energy (RCCSDa.jl:46-89)
+    # are the same number on the same factors
+    from oracle import rmp2
+    inp = inputs(1, df=True)
+    e_pair = rmp2.rmp2_energy_df(inp.Bov, inp.eps_o, inp.eps_v)
+    I = R.df_blocks(inp.Boo, inp.Bov, inp.Bvv)
+    D1, D2 = R.denominators(inp.eps_o, inp.eps_v)
+    T1, T2 = R.mp2_guess(I, D1, D2)
+    e_guess = R.cc_update_energy(T1, T2, I["OVOV"])
+    assert abs(e_pair - e_guess) < 1e-13
