@@ -45,6 +45,10 @@ MAX_RMS = 1e-8
 # one-iteration CPU sample to a full solve.
 FP64_ITERATIONS = 19
 FP64_PEAK_TFLOPS = 1.05     # measured DMMA / DFMA peak of this GB300 pool (own probe)
+# DRAM traffic per algorithmic flop of the DMMA kernel, from one ncu capture of
+# its largest launch (the o^3 v^3 ring contraction at (H2O)8, M = N = K = 4864:
+# dram__bytes_read + dram__bytes_write = 7.114e9 + 0.186e9 B for 2 * 4864^3 flop)
+DMMA_DRAM_BYTES_PER_FLOP = (7.114e9 + 0.186e9) / (2.0 * 4864.0 ** 3)
 
 
 def parse():
@@ -300,7 +304,10 @@ def main():
     ach = work / ms / (1e9 if dom != 2 else 1e6) if ms else None
     roof = {"bound": "hbm" if dom == 2 else "tensor", "kernel": cls[dom], "achieved": ach,
             "peak": peaks[dom][0], "unit": peaks[dom][1], "frac": (ach / peaks[dom][0]) if ach else None,
-            "traffic": None, "launches": int(n), "work_per_launch": (work / n) if n else None,
+            "traffic": (DMMA_DRAM_BYTES_PER_FLOP * work / n) if (dom == 0 and n) else None,
+            "traffic_note": ("bytes per average launch: the ncu-measured DRAM bytes per flop of the largest "
+                             "launch times the average launch's flops" if dom == 0 else None),
+            "launches": int(n), "work_per_launch": (work / n) if n else None,
             "peak_source": ("own measurement (DMMA probe; MEASURED_PEAKS.json has no FP64 figure)" if dom == 0
                             else "MEASURED_PEAKS.json"),
             "note": "achieved = sum of 2*M*N*K (algorithmic) over launches / sum of launch times"}

@@ -84,6 +84,38 @@ void common_tail(fcc_ctx* c, const double* eps_o, const double* eps_v, double e_
   c->have_ccsd = false;
 }
 
+// b[Q,mu,nu] (device, column-major) -> c->B over the active MO range, then the
+// common setup; Bmn (and t) are freed on return
+int upload_ao_common(fcc_ctx* c, fcc::DBuf<double>& dB, const double* C, int32_t nbf, int32_t nmo, int32_t core,
+                     int32_t ndocc, const double* eps, double e_ref) {
+  const int64_t Q = c->Q, n = c->n;
+  const int64_t nb = nbf;
+  fcc::DBuf<double> dC, t;
+  dC.alloc(nb * nmo);
+  FCC_CUDA(cudaMemcpyAsync(dC.p, C, sizeof(double) * nb * nmo, cudaMemcpyHostToDevice, c->stream));
+  // column-major views: b[Q, mu, nu] (Q fastest), C[mu, p] (mu fastest); active p in [core, core + n)
+  TView b = cm(dB.p, {Q, nb, nb});
+  TView Ca = slice(cm(dC.p, {nb, (int64_t)nmo}), 1, core, n);
+  t.alloc(Q * nb * n);
+  TView tv = rm(t.p, {Q, nb, n});
+  fcc::einsum(1.0, "Qmn,nq->Qmq", b, Ca, 0.0, tv, c->stream);
+  c->B.alloc(Q * n * n);
+  fcc::einsum(1.0, "mp,Qmq->Qpq", Ca, tv, 0.0, rm(c->B.p, {Q, n, n}), c->stream);
+  FCC_CUDA(cudaStreamSynchronize(c->stream));
+  common_tail(c, eps + core, eps + ndocc, e_ref);
+  return FCC_OK;
+}
+
+void check_ao_ranges(fcc_ctx* c, const void* a, const void* C, const double* eps, int32_t nbf, int32_t nmo, int32_t core,
+                     int32_t ndocc, double e_ref) {
+  if (!a || !C || !eps) fcc::fail(FCC_ERR_BAD_ARG, "null input");
+  if (c->Q <= 0) fcc::fail(FCC_ERR_STATE, "context created with naux = 0 (conventional); use fcc_upload_conv");
+  if (nbf <= 0 || nmo <= 0 || nmo > nbf || core < 0 || ndocc - core != c->o || ndocc + c->v > nmo)
+    fcc::fail(FCC_ERR_BAD_ARG, "orbital ranges do not match the context (ndocc - core = o, ndocc + v <= nmo)");
+  if (!finite_all(eps, nmo) || !std::isfinite(e_ref)) fcc::fail(FCC_ERR_BAD_ARG, "non-finite orbital or reference energy");
+}
+
+
 }  // namespace
 
 extern "C" {
@@ -174,6 +206,50 @@ int fcc_upload_df(fcc_ctx* c, const double* Boo, const double* Bov, const double
     fcc::einsum1(1.0, "Qia->Qai", blk(0, o, o, v), 0.0, blk(o, v, 0, o), c->stream);
     common_tail(c, eps_o, eps_v, e_ref);
     return FCC_OK;
+  });
+}
+
+// AO three-index factors and MO coefficients: the MO transform of
+// DFERI.jl:15-69 (BOO, BOV, BVV from aoints["ERI"] and the orbitals) runs on
+// the device as two FP64 contractions over the active orbital range,
+//   t[Q,mu,q] = sum_nu b[Q,mu,nu] C[nu,q],   B[Q,p,q] = sum_mu C[mu,p] t[Q,mu,q],
+// which yields the full factor (OO, OV, VO, VV blocks) at once.
+// AO three-index integrals (pq|P) and the fitting metric J^-1/2: the fit of
+// AtomicIntegrals.jl:37-38, b[Q,p,q] = sum_P (pq|P) [J^-1/2]_PQ, on the device,
+// then the MO transform below.
+int fcc_upload_ao3_df(fcc_ctx* c, const double* Pqp, const double* Jh, const double* C, int32_t nbf, int32_t nmo,
+                      int32_t core, int32_t ndocc, const double* eps, double e_ref) {
+  if (!c) return FCC_ERR_BAD_ARG;
+  return guarded(c, [&]() {
+    check_ao_ranges(c, Pqp, C, eps, nbf, nmo, core, ndocc, e_ref);
+    if (!Jh) fcc::fail(FCC_ERR_BAD_ARG, "null input");
+    const int64_t Q = c->Q, nb = nbf;
+    fcc::DBuf<double> dB;
+    {
+      fcc::DBuf<double> dP, dJ;
+      dP.alloc(nb * nb * Q);
+      dJ.alloc(Q * Q);
+      FCC_CUDA(cudaMemcpyAsync(dP.p, Pqp, sizeof(double) * nb * nb * Q, cudaMemcpyHostToDevice, c->stream));
+      FCC_CUDA(cudaMemcpyAsync(dJ.p, Jh, sizeof(double) * Q * Q, cudaMemcpyHostToDevice, c->stream));
+      dB.alloc(Q * nb * nb);
+      // Pqp[p, q, P] and Jh[P, Q] column-major; b written column-major [Q, p, q]
+      fcc::einsum(1.0, "pqP,PQ->Qpq", cm(dP.p, {nb, nb, Q}), cm(dJ.p, {Q, Q}), 0.0, cm(dB.p, {Q, nb, nb}), c->stream);
+      FCC_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return upload_ao_common(c, dB, C, nbf, nmo, core, ndocc, eps, e_ref);
+  });
+}
+
+int fcc_upload_ao_df(fcc_ctx* c, const double* Bmn, const double* C, int32_t nbf, int32_t nmo, int32_t core,
+                     int32_t ndocc, const double* eps, double e_ref) {
+  if (!c) return FCC_ERR_BAD_ARG;
+  return guarded(c, [&]() {
+    check_ao_ranges(c, Bmn, C, eps, nbf, nmo, core, ndocc, e_ref);
+    const int64_t Q = c->Q, nb = nbf;
+    fcc::DBuf<double> dB;
+    dB.alloc(Q * nb * nb);
+    FCC_CUDA(cudaMemcpyAsync(dB.p, Bmn, sizeof(double) * Q * nb * nb, cudaMemcpyHostToDevice, c->stream));
+    return upload_ao_common(c, dB, C, nbf, nmo, core, ndocc, eps, e_ref);
   });
 }
 

@@ -30,7 +30,7 @@ EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv",
            "fcc_gemm_f64_noalloc", "fcc_mlp_num_params", "fcc_mlp_create", "fcc_mlp_destroy", "fcc_mlp_get_params",
            "fcc_mlp_set_params", "fcc_mlp_collect", "fcc_mlp_train", "fcc_mlp_grad", "fcc_mlp_guess",
            "fcc_mlp_guess_ex", "fcc_checkpoint_save", "fcc_checkpoint_load", "fcc_set_checkpoint",
-           "fcc_mp2_energy")
+           "fcc_mp2_energy", "fcc_upload_ao_df", "fcc_upload_ao3_df")
 TEST_EXPORTS = ("fcc_test_contract", "fcc_stat_launches", "fcc_stream", "fcc_prof_enable", "fcc_prof_read")
 
 
@@ -117,11 +117,14 @@ def load():
     lib.fcc_stream.argtypes = [vp]
     lib.fcc_stream.restype = ctypes.c_void_p
     lib.fcc_mp2_energy.argtypes = [vp, dp]
+    lib.fcc_upload_ao_df.argtypes = [vp, dp, dp, i32, i32, i32, i32, dp, ctypes.c_double]
+    lib.fcc_upload_ao3_df.argtypes = [vp, dp, dp, dp, i32, i32, i32, i32, dp, ctypes.c_double]
     lib.fcc_checkpoint_save.argtypes = [vp, ctypes.c_char_p]
     lib.fcc_checkpoint_load.argtypes = [vp, ctypes.c_char_p]
     lib.fcc_set_checkpoint.argtypes = [vp, ctypes.c_char_p, i32]
     for name in ("fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess", "fcc_ccsd_run",
-                 "fcc_get_amps", "fcc_triples", "fcc_checkpoint_save", "fcc_checkpoint_load", "fcc_set_checkpoint", "fcc_mp2_energy"):
+                 "fcc_get_amps", "fcc_triples", "fcc_checkpoint_save", "fcc_checkpoint_load", "fcc_set_checkpoint", "fcc_mp2_energy",
+                 "fcc_upload_ao_df", "fcc_upload_ao3_df"):
         getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib

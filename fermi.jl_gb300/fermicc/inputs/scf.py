@@ -49,6 +49,10 @@ class CCInputs:
     Bvv: np.ndarray | None = None
     conv: dict | None = None
     meta: dict = field(default_factory=dict)
+    # AO-side data of the DF path (aoints["ERI"] = b[Q,mu,nu], the RHF
+    # coefficients C[mu,p], all orbital energies, ndocc, frozen core), kept when
+    # the MO transform is to run on the device
+    ao: dict | None = None
 
 
 def _sym_inv_sqrt(M: np.ndarray, what: str, tol: float = 1e-12) -> np.ndarray:
@@ -134,8 +138,9 @@ def _setup(atoms):
     return bohr, xyz, Z, orb, S, H, f, ndocc, frozen
 
 
-def df_inputs(atoms, frozen_core: bool = True) -> CCInputs:
-    """DF-RHF on the stand-in basis, then BOO/BOV/BVV with the core dropped."""
+def df_inputs(atoms, frozen_core: bool = True, keep_ao: bool = False) -> CCInputs:
+    """DF-RHF on the stand-in basis, then BOO/BOV/BVV with the core dropped
+    (and, with keep_ao, the AO factors and orbitals for a device MO transform)."""
     bohr, xyz, Z, orb, S, H, f, ndocc, frozen = _setup(atoms)
     if not frozen_core:
         frozen = 0
@@ -148,6 +153,7 @@ def df_inputs(atoms, frozen_core: bool = True) -> CCInputs:
     n, naux = orb.nbf, aux.nbf
     # b[Q, mu, nu] = sum_P (mu nu|P) Jh[P, Q]
     b = (I3.reshape(n * n, naux) @ Jh).T.reshape(naux, n, n)
+    I3_kept = I3 if keep_ao else None
     del I3
     bflat = b.reshape(naux, n * n)
 
@@ -175,7 +181,9 @@ def df_inputs(atoms, frozen_core: bool = True) -> CCInputs:
                     e_ref=E, e_nuc=e_nuc,
                     Boo=np.ascontiguousarray(Boo), Bov=np.ascontiguousarray(Bov),
                     Bvv=np.ascontiguousarray(Bvv),
-                    meta=dict(nbf=n, ndocc=ndocc, frozen=frozen, scf_iters=nit, kind="df"))
+                    meta=dict(nbf=n, ndocc=ndocc, frozen=frozen, scf_iters=nit, kind="df"),
+                    ao=(dict(Bmn=b, Pqp=I3_kept, Jh=Jh, C=C, eps=eps.copy(), ndocc=ndocc, core=frozen)
+                        if keep_ao else None))
 
 
 def conv_inputs(atoms, frozen_core: bool = False) -> CCInputs:
@@ -208,12 +216,12 @@ def conv_inputs(atoms, frozen_core: bool = False) -> CCInputs:
                     meta=dict(nbf=n, ndocc=ndocc, frozen=frozen, scf_iters=nit, kind="conv"))
 
 
-def water_inputs(n: int, seed: int = 0, df: bool = True) -> CCInputs:
+def water_inputs(n: int, seed: int = 0, df: bool = True, keep_ao: bool = False) -> CCInputs:
     """The workloads: n = 1 (README water, conventional, no frozen core) or a
     seeded (H2O)n cluster with DF and one frozen core orbital per oxygen."""
     atoms = waters(n, seed)
     if df:
-        out = df_inputs(atoms, frozen_core=(n > 1))
+        out = df_inputs(atoms, frozen_core=(n > 1), keep_ao=keep_ao)
     else:
         out = conv_inputs(atoms, frozen_core=False)
     out.meta.update(waters=n, seed=seed)

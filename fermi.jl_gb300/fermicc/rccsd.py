@@ -85,7 +85,11 @@ def _check(lib, ctx, rc, what):
 class Context:
     """One device-side coupled-cluster problem (an ``fcc_ctx``)."""
 
-    def __init__(self, moints, device: int | None = None):
+    def __init__(self, moints, device: int | None = None, mo_transform: bool = False, fit: bool = False):
+        """mo_transform: build the MO factors on the device from moints.ao
+        (aoints["ERI"] and the orbitals, the DFERI.jl:15-69 transform) instead
+        of uploading BOO/BOV/BVV; with fit, from the AO integrals (pq|P) and
+        J^-1/2 (the AtomicIntegrals.jl:37-38 fit on the device as well)."""
         self.lib = _lib.load()
         self.o, self.v = int(moints.o), int(moints.v)
         naux = int(moints.naux) if moints.Bvv is not None else 0
@@ -96,7 +100,25 @@ class Context:
         self.h = h
         eo = np.ascontiguousarray(moints.eps_o, dtype=np.float64)
         ev = np.ascontiguousarray(moints.eps_v, dtype=np.float64)
-        if naux > 0:
+        if naux > 0 and mo_transform:
+            ao = getattr(moints, "ao", None)
+            if ao is None:
+                raise FermiException("mo_transform needs the AO factors and orbitals (moints.ao)")
+            C = np.asfortranarray(ao["C"], dtype=np.float64)
+            eps = np.ascontiguousarray(ao["eps"], dtype=np.float64)
+            nbf, nmo = C.shape
+            if fit:
+                P = np.asfortranarray(ao["Pqp"], dtype=np.float64)      # [p, q, P], p fastest
+                Jh = np.asfortranarray(ao["Jh"], dtype=np.float64)
+                rc = self.lib.fcc_upload_ao3_df(h, _ptr(P), _ptr(Jh), _ptr(C), nbf, nmo, int(ao["core"]),
+                                                int(ao["ndocc"]), _ptr(eps), float(moints.e_ref))
+                _check(self.lib, h, rc, "fcc_upload_ao3_df")
+            else:
+                b = np.asfortranarray(ao["Bmn"], dtype=np.float64)   # [Q, mu, nu], Q fastest
+                rc = self.lib.fcc_upload_ao_df(h, _ptr(b), _ptr(C), nbf, nmo, int(ao["core"]), int(ao["ndocc"]),
+                                               _ptr(eps), float(moints.e_ref))
+                _check(self.lib, h, rc, "fcc_upload_ao_df")
+        elif naux > 0:
             Boo = np.asfortranarray(moints.Boo, dtype=np.float64)
             Bov = np.asfortranarray(moints.Bov, dtype=np.float64)
             Bvv = np.asfortranarray(moints.Bvv, dtype=np.float64)

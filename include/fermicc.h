@@ -108,6 +108,22 @@ int fcc_create(fcc_ctx** out, int32_t o, int32_t v, int32_t naux, int32_t device
 int fcc_upload_df(fcc_ctx* ctx, const double* Boo, const double* Bov, const double* Bvv,
                   const double* eps_o, const double* eps_v, double e_ref);
 
+/* The MO transform on the device instead (DFERI.jl:15-69 replaced): Bmn is
+ * Fermi's aoints["ERI"], b[Q,mu,nu] = sum_P (mu nu|P) [J^-1/2]_PQ
+ * (AtomicIntegrals.jl:31-40), naux x nbf x nbf column-major; C the RHF
+ * coefficients (nbf x nmo, column-major); the active occupied orbitals are
+ * [core, ndocc) (core = drop_occ) and the virtuals [ndocc, ndocc + v); eps
+ * the nmo orbital energies. */
+int fcc_upload_ao_df(fcc_ctx* ctx, const double* Bmn, const double* C, int32_t nbf, int32_t nmo, int32_t core,
+                     int32_t ndocc, const double* eps, double e_ref);
+
+/* Both DF steps on the device: Pqp the AO three-index integrals (pq|P),
+ * nbf x nbf x naux column-major, and Jh = J^-1/2 of the fitting metric
+ * (naux x naux), from which b[Q,p,q] = sum_P (pq|P) Jh[P,Q]
+ * (AtomicIntegrals.jl:37-38); then as fcc_upload_ao_df. */
+int fcc_upload_ao3_df(fcc_ctx* ctx, const double* Pqp, const double* Jh, const double* C, int32_t nbf, int32_t nmo,
+                      int32_t core, int32_t ndocc, const double* eps, double e_ref);
+
 /* Conventional MO blocks in chemist's notation, column-major:
  * OOOO[i,j,k,l] = (ij|kl), OOOV[i,j,k,a], OOVV[i,j,a,b], OVOV[i,a,j,b],
  * OVVV[i,a,b,c], VVVV[a,b,c,d].  Intended for small molecules. */
