@@ -53,6 +53,7 @@ struct fcc_ctx {
   // periodic checkpoint of fcc_ccsd_run (empty path: off)
   std::string ckpt_path;
   int32_t ckpt_every = 0;
+  int t3_bn_override = 0;     // test hook: B tile width of the mixed (T) GEMM (0: by v)
 
   // (T) scratch
   fcc::DBuf<double> ovvv, ooov, Wt;

@@ -21,11 +21,12 @@ struct T3Params {
   CUtensorMap maps[7];
   T3Seg seg[3][T3_NSEG];
   int i, j, k0, nk, o, v;
+  int bn;      // B tile width: 128, 160, 192 or 256 (t3_bn(v) unless set for a test)
   float* G;    // G[g][k - k0][v*v][v], FP32
   int* err;    // set to 1 if a bounded wait gave up
 };
 
-// the B tile width used for v virtuals (0: unsupported, v > 256)
+// the B tile width used for v virtuals (256 with several column tiles above 256)
 int t3_bn(int v);
 void gemm_t3(const T3Params& P, cudaStream_t s);
 

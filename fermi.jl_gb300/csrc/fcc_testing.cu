@@ -31,6 +31,12 @@ extern "C" int64_t fcc_stat_launches(void) { return fcc::launch_count(); }
 
 extern "C" void* fcc_stream(const fcc_ctx* c) { return c ? (void*)fcc_stream_of(c) : nullptr; }
 
+extern "C" int fcc_test_set_t3_bn(fcc_ctx* c, int32_t bn) {
+  if (!c || !(bn == 0 || bn == 128 || bn == 160 || bn == 192 || bn == 256)) return FCC_ERR_BAD_ARG;
+  c->t3_bn_override = bn;
+  return FCC_OK;
+}
+
 extern "C" int fcc_test_contract(int32_t precision, const char* spec, const double* A, const int64_t* adims,
                                  int32_t arank, const double* B, const int64_t* bdims, int32_t brank, double* C,
                                  const int64_t* cdims, int32_t crank, double alpha, double beta) {

@@ -44,14 +44,16 @@ struct T3Cfg {
 
 __device__ __forceinline__ int t3_sel(int code, int i, int j, int k) { return code == 0 ? i : (code == 1 ? j : k); }
 
-// tile t -> (m-tile, group, k - k0), m-tile fastest
+// tile t -> (m-tile, n-tile, group, k - k0), m-tile fastest
 struct T3Tile {
-  int mt, g, kq;
+  int mt, nt, g, kq;
 };
-__device__ __forceinline__ T3Tile t3_tile(int t, int tm) {
+__device__ __forceinline__ T3Tile t3_tile(int t, int tm, int tn) {
   T3Tile r;
   r.mt = t % tm;
-  const int q = t / tm;
+  int q = t / tm;
+  r.nt = q % tn;
+  q /= tn;
   r.g = q % 3;
   r.kq = q / 3;
   return r;
@@ -63,7 +65,7 @@ __device__ __forceinline__ T3Tile t3_tile(int t, int tm) {
 // warps store tile t while the MMAs of tile t+1 run.
 template <int BN>
 __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_constant__ T3Params P, int tm,
-                                                                 int ntiles) {
+                                                                 int tn, int ntiles) {
   using Cfg = T3Cfg<BN>;
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[Cfg::STAGES];
@@ -110,13 +112,14 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
     int it = 0;
     bool stop = false;
     for (int t = blockIdx.x; t < ntiles && !stop; t += gridDim.x) {
-      const T3Tile tl = t3_tile(t, tm);
+      const T3Tile tl = t3_tile(t, tm, tn);
       const int kk = P.k0 + tl.kq;
       const int64_t m0 = (int64_t)tl.mt * T3_BM;
       for (int s = 0; s < T3_NSEG && !stop; ++s) {
         const T3Seg sg = P.seg[tl.g][s];
         const int32_t arow = (int32_t)(t3_sel(sg.asel, P.i, P.j, kk) * v * v + m0);
-        const int32_t brow = (int32_t)((t3_sel(sg.bsel1, P.i, P.j, kk) * o + t3_sel(sg.bsel2, P.i, P.j, kk)) * v);
+        const int32_t brow =
+            (int32_t)((t3_sel(sg.bsel1, P.i, P.j, kk) * o + t3_sel(sg.bsel2, P.i, P.j, kk)) * v + (int64_t)tl.nt * BN);
         for (int kb = 0; kb < sg.nkb; ++kb, ++it) {
           const int st = it % Cfg::STAGES;
           const uint32_t ph = (it / Cfg::STAGES) & 1;
@@ -140,7 +143,7 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
     int it = 0, lt = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++lt) {
-      const int g = t3_tile(t, tm).g;
+      const int g = t3_tile(t, tm, tn).g;
       int total = 0;
       for (int s = 0; s < T3_NSEG; ++s) total += P.seg[g][s].nkb;
       const int b = lt & 1;
@@ -178,7 +181,7 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
     float (*tile)[33] = epi_tile[q];
     int lt = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
-      const T3Tile tl = t3_tile(t, tm);
+      const T3Tile tl = t3_tile(t, tm, tn);
       const int b = lt & 1;
       bool ok = mbar_wait(smem_u32(&accf_bar[b]), (lt >> 1) & 1);
       ok = __all_sync(0xffffffffu, ok);
@@ -186,9 +189,10 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const int64_t m0 = (int64_t)tl.mt * T3_BM;
       float* out = P.G + ((int64_t)tl.g * P.nk + tl.kq) * v2 * v;
+      const int64_t nb0 = (int64_t)tl.nt * BN;
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 32) {
-        if (c0 >= v) break;
+        if (nb0 + c0 >= v) break;
         uint32_t r[32];
         const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * Cfg::TMEM_COLS + c0);
         asm volatile(
@@ -204,7 +208,7 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
 #pragma unroll
         for (int jj = 0; jj < 32; ++jj) tile[lane][jj] = __uint_as_float(r[jj]);
         __syncwarp();
-        const int64_t n = c0 + lane;
+        const int64_t n = nb0 + c0 + lane;
         if (n < v) {
 #pragma unroll 4
           for (int jr = 0; jr < 32; ++jr) {
@@ -237,10 +241,11 @@ void launch_t3(const T3Params& P, cudaStream_t s) {
     cudaFuncSetAttribute(gemm_t3_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM);
   });
   const int64_t tm = ((int64_t)P.v * P.v + T3_BM - 1) / T3_BM;
-  const int64_t ntiles = tm * 3 * P.nk;
+  const int64_t tn = (P.v + BN - 1) / BN;
+  const int64_t ntiles = tm * tn * 3 * P.nk;
   if (ntiles > (int64_t)1 << 30) fail(FCC_ERR_BAD_ARG, "too many (T) tiles in one launch");
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, 152);
-  gemm_t3_kernel<BN><<<grid, T3_THREADS, Cfg::SMEM, s>>>(P, (int)tm, (int)ntiles);
+  gemm_t3_kernel<BN><<<grid, T3_THREADS, Cfg::SMEM, s>>>(P, (int)tm, (int)tn, (int)ntiles);
   FCC_CHECK_LAUNCH();
 }
 
@@ -250,8 +255,7 @@ int t3_bn(int v) {
   if (v <= 128) return 128;
   if (v <= 160) return 160;
   if (v <= 192) return 192;
-  if (v <= 256) return 256;
-  return 0;
+  return 256;   // v > 256: several column tiles
 }
 
 void gemm_t3(const T3Params& P, cudaStream_t s) {
@@ -260,12 +264,12 @@ void gemm_t3(const T3Params& P, cudaStream_t s) {
   const double flops = 2.0 * 3.0 * (double)P.nk * (double)P.v * P.v * P.v *
                        (double)(P.seg[0][0].nkb + P.seg[0][1].nkb + P.seg[0][2].nkb + P.seg[0][3].nkb) * T3_BK;
   const int pidx = prof_begin(s);
-  switch (t3_bn(P.v)) {
+  switch (P.bn) {
     case 128: launch_t3<128>(P, s); break;
     case 160: launch_t3<160>(P, s); break;
     case 192: launch_t3<192>(P, s); break;
     case 256: launch_t3<256>(P, s); break;
-    default: fail(FCC_ERR_BAD_ARG, "the (T) tensor-core path needs v <= 256");
+    default: fail(FCC_ERR_BAD_ARG, "no (T) tile width for this v");
   }
   prof_end(s, pidx, PROF_TC, flops);
 }

@@ -212,8 +212,7 @@ PackSpec pspec(int64_t d1, int64_t d2, int64_t d3, int64_t s1, int64_t s2, int64
 double triples_mixed(fcc_ctx* c) {
   cudaStream_t s = c->stream;
   const int64_t o = c->o, v = c->v, Q = c->Q, n = c->n;
-  const int bn = t3_bn((int)v);
-  if (bn == 0) fail(FCC_ERR_BAD_ARG, "the mixed (T) needs v <= 256");
+  const int bn = c->t3_bn_override ? c->t3_bn_override : t3_bn((int)v);
   TView B = rm(c->B.p, {Q, n, n});
   TView Boo = slice(slice(B, 1, 0, o), 2, 0, o);
   TView Bov = slice(slice(B, 1, 0, o), 2, o, v);
@@ -284,6 +283,7 @@ double triples_mixed(fcc_ctx* c) {
   P.seg[2][3] = seg(P3TA, SK, OORB, SJ, SI);
   P.o = (int)o;
   P.v = (int)v;
+  P.bn = bn;
   P.err = err;
 
   // sub-cube list of the energy kernel

@@ -31,7 +31,8 @@ EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv",
            "fcc_mlp_set_params", "fcc_mlp_collect", "fcc_mlp_train", "fcc_mlp_grad", "fcc_mlp_guess",
            "fcc_mlp_guess_ex", "fcc_checkpoint_save", "fcc_checkpoint_load", "fcc_set_checkpoint",
            "fcc_mp2_energy", "fcc_upload_ao_df", "fcc_upload_ao3_df")
-TEST_EXPORTS = ("fcc_test_contract", "fcc_stat_launches", "fcc_stream", "fcc_prof_enable", "fcc_prof_read")
+TEST_EXPORTS = ("fcc_test_contract", "fcc_stat_launches", "fcc_stream", "fcc_prof_enable", "fcc_prof_read",
+                "fcc_test_set_t3_bn")
 
 
 class FccOpts(ctypes.Structure):
@@ -114,6 +115,8 @@ def load():
     lib.fcc_prof_enable.restype = ctypes.c_int
     lib.fcc_prof_read.argtypes = [dp, i32]
     lib.fcc_prof_read.restype = ctypes.c_int
+    lib.fcc_test_set_t3_bn.argtypes = [vp, i32]
+    lib.fcc_test_set_t3_bn.restype = ctypes.c_int
     lib.fcc_stream.argtypes = [vp]
     lib.fcc_stream.restype = ctypes.c_void_p
     lib.fcc_mp2_energy.argtypes = [vp, dp]

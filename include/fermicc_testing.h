@@ -33,6 +33,10 @@ int64_t fcc_stat_launches(void);
 typedef struct fcc_ctx fcc_ctx;
 void* fcc_stream(const fcc_ctx* ctx);
 
+/* Force the B tile width (128, 160, 192, 256; 0 = chosen from v) of the mixed
+ * (T) GEMM, e.g. to run several column tiles on a small system. */
+int fcc_test_set_t3_bn(fcc_ctx* ctx, int32_t bn);
+
 /* Opt-in per-class kernel timing with CUDA events on the launching stream:
  * classes 0 FP64 contractions (work = 2MNK flop), 1 tensor-core GEMMs (work =
  * executed BF16 flop), 2 operand packing (work = bytes), 3 updates, 4 (T)

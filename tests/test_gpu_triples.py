@@ -40,3 +40,26 @@ def test_triples_mixed_close_to_fp64(case):
     emx = RCCSDpT.compute(ccsd, inp).correction
     assert abs(emx - e64) < 1e-6
     assert abs(emx - e64) < 1e-4 * abs(e64)
+
+
+def test_triples_mixed_column_tiles_give_the_same_energy():
+    # (H2O)8 has v = 152: the default tile width 160 covers it in one column
+    # tile; width 128 needs two.  Same products in the same K order: the
+    # energies agree to rounding.
+    from conftest import inputs
+    from fermicc import Options, RCCSD, _lib
+    from fermicc.rccsd import Context
+    inp = inputs(8)
+    Options.reset()
+    Options.set("cc_gpu_precision", "mixed")
+    Options.set("cc_max_iter", 2)
+    ctx = Context(inp)
+    RCCSD.compute(inp, context=ctx)
+    lib = _lib.load()
+    e160 = ctx.triples(_lib.FCC_PREC_MIXED)
+    assert lib.fcc_test_set_t3_bn(ctx.h, 128) == 0
+    e128 = ctx.triples(_lib.FCC_PREC_MIXED)
+    assert lib.fcc_test_set_t3_bn(ctx.h, 0) == 0
+    assert abs(e128 - e160) < 1e-11, (e128, e160)
+    ctx.close()
+    Options.reset()
