@@ -548,12 +548,15 @@ void gemm_oz(const __nv_bfloat16* A, int64_t a_rows, const int* exA, const __nv_
   const int64_t tm = (ep.M + OZ_BM - 1) / OZ_BM, tn = (ep.N + OZ_BN - 1) / OZ_BN;
   const int64_t tiles = tm * tn;
   const int total = pr.n * nkb;
-  // split the step sequence over CTAs when that shortens the last wave
+  // split the step sequence over CTAs when that shortens the last wave; a CTA
+  // also pays a fixed cost (prologue, final epilogue, reductions into C) of
+  // about 48 k-block steps, so splits stop paying before the waves even out
   int splits = 1;
   double best = 1e300;
+  constexpr double CTA_FIXED_STEPS = 48.0;
   for (int sp = 1; sp <= 64 && sp * OZ_CH <= total; ++sp) {
     const double waves = std::ceil((double)(tiles * sp) / 152.0);
-    const double t = waves / sp;
+    const double t = waves * ((double)total / sp + CTA_FIXED_STEPS);
     if (t < best * 0.97) { best = t; splits = sp; }
   }
   const int per = (total + splits - 1) / splits;

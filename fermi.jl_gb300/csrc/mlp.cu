@@ -243,20 +243,6 @@ __global__ void gather_kernel(const float* X, const float* Y, int64_t B, uint64_
   }
 }
 
-// MP2 + lam * learned correction into t2 for the elements with
-// |t_MP2| >= thresh (the others keep their MP2 value); t1 = 0.
-__global__ void infer_write_kernel(FeatSrc f, const float* y, int64_t base, int64_t n, double lam, double thresh,
-                                   double* t2) {
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t e = base + s;
-    float x[NF];
-    double tmp2;
-    features(f, e, x, tmp2);
-    const double corr = fabs(tmp2) >= thresh ? lam * (double)y[s] * (fabs(tmp2) + TARGET_FLOOR) : 0.0;
-    t2[e] = tmp2 + corr;
-  }
-}
-
 // t_ijab = t_jiba holds for the exact amplitudes; the network sees the two
 // elements through different feature vectors, so average them.
 __global__ void pair_symmetrise_kernel(double* t2, int o, int v) {
@@ -276,12 +262,50 @@ __global__ void pair_symmetrise_kernel(double* t2, int o, int v) {
   }
 }
 
-__global__ void infer_features_kernel(FeatSrc f, int64_t base, int64_t n, const float* mu, const float* sd, float* Xn) {
+// t2 = t_MP2 for every element; the elements with |t_MP2| >= thresh (the
+// ones the correction is applied to) are appended to sel (in any order: each
+// gets its own prediction, so the result does not depend on the order)
+__global__ void mp2_select_kernel(FeatSrc f, int64_t total, double thresh, double* t2, int64_t* sel,
+                                  unsigned long long* nsel) {
+  __shared__ unsigned int cnt, base;
+  for (int64_t e0 = (int64_t)blockIdx.x * blockDim.x; e0 < total; e0 += (int64_t)gridDim.x * blockDim.x) {
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
+    const int64_t e = e0 + threadIdx.x;
+    unsigned int slot = 0;
+    bool take = false;
+    if (e < total) {
+      float x[NF];
+      double tmp2;
+      features(f, e, x, tmp2);
+      t2[e] = tmp2;
+      take = fabs(tmp2) >= thresh;
+      if (take) slot = atomicAdd(&cnt, 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) base = cnt ? (unsigned int)atomicAdd(nsel, (unsigned long long)cnt) : 0u;
+    __syncthreads();
+    if (take) sel[(int64_t)base + slot] = e;
+    __syncthreads();
+  }
+}
+
+__global__ void infer_features_sel_kernel(FeatSrc f, const int64_t* sel, int64_t n, const float* mu, const float* sd,
+                                          float* Xn) {
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
     float x[NF];
     double tmp2;
-    features(f, base + s, x, tmp2);
+    features(f, sel[s], x, tmp2);
     for (int q = 0; q < NF; ++q) Xn[s * NF + q] = (x[q] - mu[q]) / sd[q];
+  }
+}
+
+// t2 += lam * correction for the selected elements
+__global__ void infer_write_sel_kernel(const float* y, const int64_t* sel, int64_t n, double lam, double* t2) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = sel[s];
+    const double tmp2 = t2[e];
+    t2[e] = tmp2 + lam * (double)y[s] * (fabs(tmp2) + TARGET_FLOOR);
   }
 }
 
@@ -607,12 +631,26 @@ int fcc_mlp_guess_ex(fcc_ctx* c, const fcc_mlp* mc, double lam, double thresh) {
     DBuf<double> pn;
     FeatSrc f = feat_src(c, pn);
     FCC_CUDA(cudaStreamSynchronize(c->stream));
-    for (int64_t base = 0; base < total; base += chunk) {
-      const int64_t nb = std::min(chunk, total - base);
-      infer_features_kernel<<<grid_of(nb), 256, 0, s>>>(f, base, nb, m->p.p + OFF_MU, m->p.p + OFF_SD, m->Xb.p);
+    // MP2 everywhere; the network runs only on the elements whose correction
+    // is applied (|t_MP2| >= thresh), compacted into sel
+    DBuf<int64_t> sel;
+    DBuf<unsigned long long> nsel;
+    sel.alloc(total);
+    nsel.alloc(1);
+    FCC_CUDA(cudaMemsetAsync(nsel.p, 0, sizeof(unsigned long long), s));
+    mp2_select_kernel<<<grid_of(total), 256, 0, s>>>(f, total, thresh, c->t2.p, sel.p, nsel.p);
+    FCC_CHECK_LAUNCH();
+    unsigned long long hsel = 0;
+    FCC_CUDA(cudaMemcpyAsync(&hsel, nsel.p, sizeof(hsel), cudaMemcpyDeviceToHost, s));
+    FCC_CUDA(cudaStreamSynchronize(s));
+    const int64_t nsel_h = (int64_t)hsel;
+    for (int64_t base = 0; base < nsel_h && lam != 0.0; base += chunk) {
+      const int64_t nb = std::min(chunk, nsel_h - base);
+      infer_features_sel_kernel<<<grid_of(nb), 256, 0, s>>>(f, sel.p + base, nb, m->p.p + OFF_MU, m->p.p + OFF_SD,
+                                                            m->Xb.p);
       FCC_CHECK_LAUNCH();
       fwd_bwd(m, nb, nullptr, false);
-      infer_write_kernel<<<grid_of(nb), 256, 0, s>>>(f, m->yb.p, base, nb, lam, thresh, c->t2.p);
+      infer_write_sel_kernel<<<grid_of(nb), 256, 0, s>>>(m->yb.p, sel.p + base, nb, lam, c->t2.p);
       FCC_CHECK_LAUNCH();
     }
     pair_symmetrise_kernel<<<grid_of(total), 256, 0, s>>>(c->t2.p, (int)c->o, (int)c->v);
