@@ -34,6 +34,39 @@ struct PackSpec {
   double scale = 1.0;   // the source is multiplied by this (exact for +-1 and powers of two)
 };
 
+// Source offsets of packed row r and packed column k (32-bit index
+// arithmetic: pack_split / pack_oz reject R or K of 2^31 or more).
+__device__ __forceinline__ int64_t pack_row_off(const PackSpec& ps, int64_t r) {
+  const uint32_t rr = (uint32_t)r, d3 = (uint32_t)ps.rd3, d2 = (uint32_t)ps.rd2;
+  const uint32_t r3 = rr % d3, q = rr / d3;
+  return (int64_t)(q / d2) * ps.rs1 + (int64_t)(q % d2) * ps.rs2 + (int64_t)r3 * ps.rs3;
+}
+__device__ __forceinline__ int64_t pack_col_off(const PackSpec& ps, int64_t k) {
+  const uint32_t kk = (uint32_t)k, d3 = (uint32_t)ps.kd3, d2 = (uint32_t)ps.kd2;
+  const uint32_t k3 = kk % d3, q = kk / d3;
+  return (int64_t)(q / d2) * ps.ks1 + (int64_t)(q % d2) * ps.ks2 + (int64_t)k3 * ps.ks3;
+}
+// Walks consecutive packed columns k, k+1, ... without divisions.
+struct PackColIter {
+  uint32_t k2, k3;
+  int64_t off;
+  __device__ __forceinline__ PackColIter(const PackSpec& ps, int64_t k) {
+    const uint32_t kk = (uint32_t)k, d3 = (uint32_t)ps.kd3, d2 = (uint32_t)ps.kd2;
+    k3 = kk % d3;
+    const uint32_t q = kk / d3;
+    k2 = q % d2;
+    off = (int64_t)(q / d2) * ps.ks1 + (int64_t)k2 * ps.ks2 + (int64_t)k3 * ps.ks3;
+  }
+  __device__ __forceinline__ void next(const PackSpec& ps) {
+    if (++k3 < (uint32_t)ps.kd3) { off += ps.ks3; return; }
+    k3 = 0;
+    off += ps.ks2 - (ps.kd3 - 1) * ps.ks3;
+    if (++k2 < (uint32_t)ps.kd2) return;
+    k2 = 0;
+    off += ps.ks1 - ps.kd2 * ps.ks2;   // from (k1, kd2, 0) to (k1 + 1, 0, 0)
+  }
+};
+
 // Output scatter of the GEMM: element (m, n) goes to
 // C[m1*ms1 + m2*ms2 + m3*ms3 + n1*ns1 + n2*ns2 + n3*ns3] as
 //   EPI_F64 / EPI_F32: alpha * acc + beta * C (atomic add when split over K);

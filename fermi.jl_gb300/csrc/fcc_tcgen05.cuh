@@ -79,6 +79,20 @@ __device__ __forceinline__ void tc_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
+// (double)f * 2^e (negated if neg) by integer exponent arithmetic; FP32
+// subnormals and results below the FP64 normal range give 0
+__device__ __forceinline__ double f32_to_f64_scaled(float f, int e, bool neg) {
+  const uint32_t b = __float_as_uint(f);
+  const int ex = (int)((b >> 23) & 0xFF);
+  if (ex == 0) return 0.0;
+  int ne = ex - 127 + 1023 + e;
+  if (ne <= 0) return 0.0;
+  if (ne > 2046) ne = 2047;
+  const unsigned long long sign = (unsigned long long)((b >> 31) ^ (neg ? 1u : 0u)) << 63;
+  const unsigned long long bits = sign | ((unsigned long long)ne << 52) | ((unsigned long long)(b & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
 // Output tile of linear block index lin on a tm x tn tile grid, walked in
 // groups of 8 tile rows (row fastest inside a group) so that the CTAs resident
 // at the same time share A and B panels in L2.

@@ -100,20 +100,6 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float v) {
   hi = h;
 }
 
-// (double)f * 2^e (negated if neg) by integer exponent arithmetic; FP32
-// subnormals and results below the FP64 normal range give 0
-__device__ __forceinline__ double f32_to_f64_scaled(float f, int e, bool neg) {
-  const uint32_t b = __float_as_uint(f);
-  const int ex = (int)((b >> 23) & 0xFF);
-  if (ex == 0) return 0.0;
-  int ne = ex - 127 + 1023 + e;
-  if (ne <= 0) return 0.0;
-  if (ne > 2046) ne = 2047;
-  const unsigned long long sign = (unsigned long long)((b >> 31) ^ (neg ? 1u : 0u)) << 63;
-  const unsigned long long bits = sign | ((unsigned long long)ne << 52) | ((unsigned long long)(b & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)bits);
-}
-
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -361,14 +347,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 
 // ---------------------------------------------------------------- packing
 
-__device__ __forceinline__ int64_t oz_row_off(const PackSpec& ps, int64_t r) {
-  const int64_t r3 = r % ps.rd3, q = r / ps.rd3;
-  return (q / ps.rd2) * ps.rs1 + (q % ps.rd2) * ps.rs2 + r3 * ps.rs3;
-}
-__device__ __forceinline__ int64_t oz_col_off(const PackSpec& ps, int64_t k) {
-  const int64_t k3 = k % ps.kd3, q = k / ps.kd3;
-  return (q / ps.kd2) * ps.ks1 + (q % ps.kd2) * ps.ks2 + k3 * ps.ks3;
-}
 __device__ __forceinline__ int biased_exp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7FF); }
 
 // ex[r] = max over the row of the biased exponent (ex zeroed before), for
@@ -379,9 +357,9 @@ __global__ void oz_exp_rows_kernel(const double* __restrict__ src, PackSpec ps, 
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < ps.R * nks; w += nw) {
     const int64_t r = w / nks, k0 = (w % nks) * kslab, k1 = min(ps.K, k0 + kslab);
-    const int64_t ro = oz_row_off(ps, r);
+    const int64_t ro = pack_row_off(ps, r);
     int m = 0;
-    for (int64_t k = k0 + lane; k < k1; k += 32) m = max(m, biased_exp(src[ro + oz_col_off(ps, k)]));
+    for (int64_t k = k0 + lane; k < k1; k += 32) m = max(m, biased_exp(src[ro + pack_col_off(ps, k)]));
     m = __reduce_max_sync(0xffffffffu, m);
     if (lane == 0 && m > 0) atomicMax(ex + r, m);
   }
@@ -398,8 +376,8 @@ __global__ void oz_exp_tiles_kernel(const double* __restrict__ src, PackSpec ps,
     const int64_t k0 = (tb % nks) * kslab, k1 = min(ps.K, k0 + kslab);
     int m = 0;
     if (r < ps.R) {
-      const int64_t ro = oz_row_off(ps, r);
-      for (int64_t k = k0 + ty; k < k1; k += 8) m = max(m, biased_exp(src[ro + oz_col_off(ps, k)]));
+      const int64_t ro = pack_row_off(ps, r);
+      for (int64_t k = k0 + ty; k < k1; k += 8) m = max(m, biased_exp(src[ro + pack_col_off(ps, k)]));
     }
     red[ty][tx] = m;
     __syncthreads();
@@ -447,10 +425,12 @@ __global__ void oz_pack_rows_kernel(const double* __restrict__ src, PackSpec ps,
     __nv_bfloat16* drow = dst + r * (S * Kpad);
     __nv_bfloat16 dg[4][OZ_MAXS];
     const int e = oz_row_exp(ex[r]);
-    const int64_t ro = oz_row_off(ps, r);
+    const int64_t ro = pack_row_off(ps, r);
+    PackColIter ci(ps, k0 < ps.K ? k0 : 0);
     for (int qq = 0; qq < 4; ++qq) {
       const int64_t k = k0 + qq;
-      oz_digits(k < ps.K ? src[ro + oz_col_off(ps, k)] : 0.0, e, S, dg[qq]);
+      oz_digits(k < ps.K ? src[ro + ci.off] : 0.0, e, S, dg[qq]);
+      if (k + 1 < ps.K) ci.next(ps);
     }
     for (int s = 0; s < S; ++s) {
       __nv_bfloat162 v0 = __halves2bfloat162(dg[0][s], dg[1][s]);
@@ -475,7 +455,7 @@ __global__ void oz_pack_tiles_kernel(const double* __restrict__ src, PackSpec ps
     for (int j = 0; j < 4; ++j) {
       const int kk = ty + 8 * j;
       const int64_t r = r0 + tx, k = k0 + kk;
-      tile[kk][tx] = (r < ps.R && k < ps.K) ? src[oz_row_off(ps, r) + oz_col_off(ps, k)] : 0.0;
+      tile[kk][tx] = (r < ps.R && k < ps.K) ? src[pack_row_off(ps, r) + pack_col_off(ps, k)] : 0.0;
     }
     __syncthreads();
     for (int j = 0; j < 4; ++j) {
@@ -499,6 +479,7 @@ int64_t oz_kpad(int64_t K) { return ((K + OZ_BK - 1) / OZ_BK) * OZ_BK; }
 void pack_oz(const double* src, const PackSpec& ps, int S, __nv_bfloat16* dst, int* ex, cudaStream_t s) {
   if (ps.R <= 0 || ps.K <= 0) return;
   if (S < 1 || S > OZ_MAXS) fail(FCC_ERR_BAD_ARG, "bad slice count");
+  if (ps.R >= (int64_t(1) << 31) || ps.K >= (int64_t(1) << 31)) fail(FCC_ERR_BAD_ARG, "pack extent too large");
   const int64_t Kpad = oz_kpad(ps.K);
   const int pidx = prof_begin(s);
   struct End { cudaStream_t s; int i; double b; ~End() { prof_end(s, i, PROF_PACK, b); } } pend{s, pidx,

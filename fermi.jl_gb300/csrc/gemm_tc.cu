@@ -184,7 +184,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         // all loads of the block first (independent, so they overlap), then
         // the stores
-        const bool rmw = ep.beta != 0.0 && !ep.atomic && ep.mode != EPI_SPLIT;
+        // FP64 outputs with beta = 1 are reduced into C (red.add, no load);
+        // only other betas read C
+        const bool rmw = ep.beta != 0.0 && !ep.atomic && ep.mode != EPI_SPLIT &&
+                         !(ep.mode == EPI_F64 && ep.beta == 1.0);
         double prev[32];
         float prevf[32];
         if (rmw) {
@@ -213,6 +216,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (rmw) fv += (float)ep.beta * prevf[jr];
             if (ep.atomic) atomicAdd(dst, fv);
             else *dst = fv;
+            continue;
+          }
+          if (ep.mode == EPI_F64) {
+            // FP32 product, converted to FP64 by integer arithmetic (the FP64
+            // pipe, which F2F conversions use, is 1/64 rate on GB300)
+            double val = f32_to_f64_scaled((float)ep.alpha * tile[jr][lane], 0, false);
+            double* dst = static_cast<double*>(ep.C) + off;
+            if (ep.atomic || ep.beta == 1.0) atomicAdd(dst, val);
+            else if (rmw) *dst = val + ep.beta * prev[jr];
+            else *dst = val;
             continue;
           }
           double val = (double)((float)ep.alpha * tile[jr][lane]);
@@ -246,15 +259,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
 // ---------------------------------------------------------------- packing
 
-__device__ __forceinline__ int64_t row_off(const PackSpec& ps, int64_t r) {
-  const int64_t r3 = r % ps.rd3, q = r / ps.rd3;
-  return (q / ps.rd2) * ps.rs1 + (q % ps.rd2) * ps.rs2 + r3 * ps.rs3;
-}
-__device__ __forceinline__ int64_t col_off(const PackSpec& ps, int64_t k) {
-  const int64_t k3 = k % ps.kd3, q = k / ps.kd3;
-  return (q / ps.kd2) * ps.ks1 + (q % ps.kd2) * ps.ks2 + k3 * ps.ks3;
-}
-
 // dst[r][k'] (row pitch Kp) from src: piece p of k' = p*K + k holds hi or lo
 // of src(r, k) per `pattern` (bit p set = lo); columns >= 3K are zero.
 // Row-major walk: each thread splits 4 consecutive k of one row once and
@@ -268,10 +272,14 @@ __global__ void pack_rows_kernel(const double* __restrict__ src, PackSpec ps, __
     const int64_t k0 = g * 4;
     __nv_bfloat16* drow = dst + r * ps.Kp;
     if (k0 < ps.K) {
-      const int64_t ro = row_off(ps, r);
+      const int64_t ro = pack_row_off(ps, r);
       __nv_bfloat16 lv[4][3];
       const int cnt = (int)min((int64_t)4, ps.K - k0);
-      for (int q = 0; q < 4; ++q) split3(q < cnt ? ps.scale * src[ro + col_off(ps, k0 + q)] : 0.0, lv[q]);
+      PackColIter ci(ps, k0);
+      for (int q = 0; q < 4; ++q) {
+        split3(q < cnt ? ps.scale * src[ro + ci.off] : 0.0, lv[q]);
+        if (q + 1 < cnt) ci.next(ps);
+      }
       for (int p = 0; p < ps.P; ++p) {
         const int lev = (ps.code >> (2 * p)) & 3;
         __nv_bfloat16* d = drow + p * ps.K + k0;
@@ -308,7 +316,7 @@ __global__ void pack_tiles_kernel(const double* __restrict__ src, PackSpec ps, _
     for (int j = 0; j < 4; ++j) {
       const int kk = ty + 8 * j;
       const int64_t r = r0 + tx, k = k0 + kk;
-      tile[kk][tx] = (r < ps.R && k < ps.K) ? ps.scale * src[row_off(ps, r) + col_off(ps, k)] : 0.0;
+      tile[kk][tx] = (r < ps.R && k < ps.K) ? ps.scale * src[pack_row_off(ps, r) + pack_col_off(ps, k)] : 0.0;
     }
     __syncthreads();
     for (int j = 0; j < 4; ++j) {
@@ -404,9 +412,11 @@ void launch_tc(const __nv_bfloat16* A, int64_t a_rows, int64_t a_row0, const __n
   splits = (num_k + chunk - 1) / chunk;
   EpiMap e2 = ep;
   if (splits > 1) {
-    const int64_t tot = ep.M * ep.N;
-    scale_out_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 152 * 16), 256, 0, s>>>(ep, ep.beta);
-    FCC_CHECK_LAUNCH();
+    if (ep.beta != 1.0) {   // C = beta * C before the partial sums are added
+      const int64_t tot = ep.M * ep.N;
+      scale_out_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 152 * 16), 256, 0, s>>>(ep, ep.beta);
+      FCC_CHECK_LAUNCH();
+    }
     e2.atomic = 1;
   }
   if (tm * tn > 2147483647ll) fail(FCC_ERR_BAD_ARG, "tensor-core grid too large");
@@ -439,6 +449,7 @@ void pack_split(const double* src, const PackSpec& ps, __nv_bfloat16* dst, cudaS
   struct End { cudaStream_t s; int i; double b; ~End() { prof_end(s, i, PROF_PACK, b); } } pend{s, pidx,
       (double)ps.R * (double)ps.K * 8.0 + (double)ps.R * (double)ps.Kp * 2.0};
   if (ps.P < 1 || ps.P > 8 || ps.Kp < ps.P * ps.K) fail(FCC_ERR_BAD_ARG, "bad pack spec");
+  if (ps.R >= (int64_t(1) << 31) || ps.K >= (int64_t(1) << 31)) fail(FCC_ERR_BAD_ARG, "pack extent too large");
   const int64_t kfast = std::llabs(ps.kd3 > 1 ? ps.ks3 : (ps.kd2 > 1 ? ps.ks2 : ps.ks1));
   const int64_t rfast = std::llabs(ps.rd3 > 1 ? ps.rs3 : (ps.rd2 > 1 ? ps.rs2 : ps.rs1));
   if (rfast < kfast && ps.R >= 32) {
