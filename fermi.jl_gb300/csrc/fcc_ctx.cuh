@@ -46,8 +46,7 @@ struct fcc_ctx {
   // split-BF16 tensor-core engine (mixed form) and its device error flag
   fcc::TcEngine tc;
   fcc::DBuf<int> dev_err;
-  // statistics of the last run
-  int64_t launches = 0;
+  // the last run
   double last_ecc = 0.0;      // correlation energy of the current amplitudes
   int32_t last_iters = 0, last_converged = 0;
   // periodic checkpoint of fcc_ccsd_run (empty path: off)

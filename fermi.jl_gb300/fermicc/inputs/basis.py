@@ -3,7 +3,7 @@
 Fermi.jl reads basis sets from Gaussian94 files through GaussianBasis.jl
 (``src/Core/Integrals/IntegralHelper.jl:79-89`` picks the orbital basis and
 the RI / JK fitting basis; ``src/Core/Integrals/ERITypes.jl:84-95`` maps
-``rifit auto`` to ``<basis>-rifit``).  No basis-set file exists in this build,
+``rifit auto`` to ``<basis>-rifit``).  No basis-set file ships with this package,
 so the coupled-cluster inputs are produced on project-defined basis sets that
 keep the published SHELL STRUCTURE and therefore the dimensions of every
 tensor on the coupled-cluster path:

@@ -1,6 +1,6 @@
 """ORACLE (test infrastructure only): CPU restatement of Fermi.jl's RCCSD.
 
-This module is the checker for the GB300 coupled-cluster path.  Only the test
+This module is the reference the GB300 coupled-cluster path is tested against.  Only the test
 suite, ``__graft_entry__.smoke()`` and the CPU-baseline legs of ``bench.py``
 may import it; the product path never calls into ``oracle/``.
 
