@@ -7,8 +7,9 @@ Fermi's method objects and options, plus the stand-in input pipeline
 """
 from . import options as Options
 from .options import FermiException
+from .rhf import RHF, DFFock, RHFcuda, get_rhf_alg
 from .rccsd import (CudaPT, RCCSD, RCCSDcuda, RCCSDpT, RMP2, RMP2cuda, energy, get_pt_alg, get_rccsd_alg,
                     get_rmp2_alg)
 
 __all__ = ["Options", "FermiException", "RCCSD", "RCCSDpT", "RCCSDcuda", "CudaPT", "RMP2", "RMP2cuda", "energy",
-           "get_rccsd_alg", "get_pt_alg", "get_rmp2_alg"]
+           "get_rccsd_alg", "get_pt_alg", "get_rmp2_alg", "RHF", "RHFcuda", "DFFock", "get_rhf_alg"]

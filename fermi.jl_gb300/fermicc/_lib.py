@@ -30,7 +30,8 @@ EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv",
            "fcc_gemm_f64_noalloc", "fcc_mlp_num_params", "fcc_mlp_create", "fcc_mlp_destroy", "fcc_mlp_get_params",
            "fcc_mlp_set_params", "fcc_mlp_collect", "fcc_mlp_train", "fcc_mlp_grad", "fcc_mlp_guess",
            "fcc_mlp_guess_ex", "fcc_checkpoint_save", "fcc_checkpoint_load", "fcc_set_checkpoint",
-           "fcc_mp2_energy", "fcc_upload_ao_df", "fcc_upload_ao3_df")
+           "fcc_mp2_energy", "fcc_upload_ao_df", "fcc_upload_ao3_df", "fcc_scf_create", "fcc_scf_destroy",
+           "fcc_scf_last_error", "fcc_scf_upload_b", "fcc_scf_fit", "fcc_scf_build_fock", "fcc_scf_build_fock_occ")
 TEST_EXPORTS = ("fcc_test_contract", "fcc_stat_launches", "fcc_stream", "fcc_prof_enable", "fcc_prof_read",
                 "fcc_test_set_t3_bn")
 
@@ -125,6 +126,17 @@ def load():
     lib.fcc_checkpoint_save.argtypes = [vp, ctypes.c_char_p]
     lib.fcc_checkpoint_load.argtypes = [vp, ctypes.c_char_p]
     lib.fcc_set_checkpoint.argtypes = [vp, ctypes.c_char_p, i32]
+    lib.fcc_scf_create.argtypes = [ctypes.POINTER(vp), i32, i32, i32]
+    lib.fcc_scf_destroy.argtypes = [vp]
+    lib.fcc_scf_destroy.restype = None
+    lib.fcc_scf_last_error.argtypes = [vp]
+    lib.fcc_scf_last_error.restype = ctypes.c_char_p
+    lib.fcc_scf_upload_b.argtypes = [vp, dp]
+    lib.fcc_scf_fit.argtypes = [vp, dp, dp]
+    lib.fcc_scf_build_fock.argtypes = [vp, dp, dp, dp, dp]
+    lib.fcc_scf_build_fock_occ.argtypes = [vp, dp, dp, i32, dp, dp]
+    for name in ("fcc_scf_create", "fcc_scf_upload_b", "fcc_scf_fit", "fcc_scf_build_fock", "fcc_scf_build_fock_occ"):
+        getattr(lib, name).restype = ctypes.c_int
     for name in ("fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess", "fcc_ccsd_run",
                  "fcc_get_amps", "fcc_triples", "fcc_checkpoint_save", "fcc_checkpoint_load", "fcc_set_checkpoint", "fcc_mp2_energy",
                  "fcc_upload_ao_df", "fcc_upload_ao3_df"):

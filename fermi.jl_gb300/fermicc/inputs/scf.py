@@ -138,12 +138,25 @@ def _setup(atoms):
     return bohr, xyz, Z, orb, S, H, f, ndocc, frozen
 
 
-def df_inputs(atoms, frozen_core: bool = True, keep_ao: bool = False) -> CCInputs:
-    """DF-RHF on the stand-in basis, then BOO/BOV/BVV with the core dropped
-    (and, with keep_ao, the AO factors and orbitals for a device MO transform)."""
+@dataclass
+class AOProblem:
+    """The AO-side inputs of a DF-RHF (the IntegralHelper cache of Fermi):
+    H = T + V, S, the fitting quantities (pq|P), J^-1/2 and
+    b[Q,mu,nu] = sum_P (mu nu|P) [J^-1/2]_PQ (AtomicIntegrals.jl:31-40), the
+    number of doubly occupied orbitals, the frozen-core count and Vnuc."""
+    H: np.ndarray
+    S: np.ndarray
+    b: np.ndarray
+    Pqp: np.ndarray | None
+    Jh: np.ndarray
+    ndocc: int
+    frozen: int
+    e_nuc: float
+
+
+def df_ao_problem(atoms, keep_pqp: bool = False) -> AOProblem:
+    """One-body matrices and DF factors of the stand-in basis for ``atoms``."""
     bohr, xyz, Z, orb, S, H, f, ndocc, frozen = _setup(atoms)
-    if not frozen_core:
-        frozen = 0
     aux = bas.flatten(bohr, bas.fitting_shells)
     J2 = ints.eri2c(aux)
     g = 1.0 / np.sqrt(np.diag(J2))
@@ -153,8 +166,19 @@ def df_inputs(atoms, frozen_core: bool = True, keep_ao: bool = False) -> CCInput
     n, naux = orb.nbf, aux.nbf
     # b[Q, mu, nu] = sum_P (mu nu|P) Jh[P, Q]
     b = (I3.reshape(n * n, naux) @ Jh).T.reshape(naux, n, n)
-    I3_kept = I3 if keep_ao else None
-    del I3
+    return AOProblem(H=H, S=S, b=b, Pqp=I3 if keep_pqp else None, Jh=Jh, ndocc=ndocc, frozen=frozen,
+                     e_nuc=_nuclear_repulsion(xyz, Z))
+
+
+def df_inputs(atoms, frozen_core: bool = True, keep_ao: bool = False) -> CCInputs:
+    """DF-RHF on the stand-in basis, then BOO/BOV/BVV with the core dropped
+    (and, with keep_ao, the AO factors and orbitals for a device MO transform)."""
+    ao = df_ao_problem(atoms, keep_pqp=keep_ao)
+    H, S, b, Jh, ndocc, frozen, e_nuc = ao.H, ao.S, ao.b, ao.Jh, ao.ndocc, ao.frozen, ao.e_nuc
+    if not frozen_core:
+        frozen = 0
+    naux, n = b.shape[0], b.shape[1]
+    I3_kept = ao.Pqp
     bflat = b.reshape(naux, n * n)
 
     def jk(D, Co):
@@ -165,7 +189,6 @@ def df_inputs(atoms, frozen_core: bool = True, keep_ao: bool = False) -> CCInput
         K = bi2 @ bi2.T
         return J, K
 
-    e_nuc = _nuclear_repulsion(xyz, Z)
     E, eps, C, nit = _scf(H, S, ndocc, jk, e_nuc)
     Co = C[:, frozen:ndocc]
     Cv = C[:, ndocc:]

@@ -19,6 +19,10 @@ keys the coupled-cluster path reads, plus the keys this backend adds:
 * ``pt_gpu_precision`` -- "fp64" or "mixed" for (T).
 * ``cc_gpu_checkpoint`` / ``cc_gpu_checkpoint_every`` -- checkpoint file of the
   amplitudes, written every N iterations and at the end of a run (0: off).
+* ``rhf_alg`` -- 3 selects this backend's DF-RHF (``RHFcuda``, device Fock
+  build); Fermi's 1-2 are its Julia ``RHFa`` / ``Direct``.  The SCF keys
+  (``scf_*``, ``diis``, ``ndiis``, ``oda*``, ``scf_guess``) keep Fermi's
+  defaults (src/Core/Options.jl:55-89).
 """
 from __future__ import annotations
 
@@ -52,6 +56,16 @@ DEFAULT = {
     "cc_gpu_device": 0,
     "cc_gpu_checkpoint": "",
     "cc_gpu_checkpoint_every": 0,
+    "rhf_alg": 3,
+    "scf_max_iter": 50,
+    "scf_max_rms": 1e-9,
+    "scf_e_conv": 1e-10,
+    "scf_guess": "gwh",
+    "diis": True,
+    "ndiis": 8,
+    "oda": True,
+    "oda_cutoff": 1e-1,
+    "oda_shutoff": 20,
 }
 
 _current: dict = {}

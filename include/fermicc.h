@@ -217,6 +217,29 @@ int fcc_mlp_guess_ex(fcc_ctx* ctx, const fcc_mlp* m, double lam, double thresh);
 int fcc_gemm_f64_noalloc(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
                          const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* stream);
 
+/* ---- DF-RHF Fock build ----------------------------------------------------
+ * Replaces build_fock!(F, H, D, ints::IntegralHelper{Float64,<:AbstractDFERI,
+ * AtomicOrbitals}) (HartreeFock/RHF/RHFHelper.jl:88-93), called from the RHF
+ * iterations (RHFa.jl:125, :150), and RHFEnergy (RHFHelper.jl:65-67).  The
+ * handle keeps b[Q,mu,nu] (aoints["ERI"]) resident on the device for the
+ * whole SCF; it is independent of an fcc_ctx. */
+typedef struct fcc_scf fcc_scf;
+int fcc_scf_create(fcc_scf** out, int32_t nbf, int32_t naux, int32_t device);
+void fcc_scf_destroy(fcc_scf* s);
+const char* fcc_scf_last_error(const fcc_scf* s);
+/* b[Q,mu,nu], naux x nbf x nbf column-major (Fermi's aoints["ERI"] in DF mode) */
+int fcc_scf_upload_b(fcc_scf* s, const double* Bmn);
+/* the fit of AtomicIntegrals.jl:37-38 on the device instead: Pqp (pq|P)
+ * nbf x nbf x naux and Jh = J^-1/2 naux x naux, both column-major */
+int fcc_scf_fit(fcc_scf* s, const double* Pqp, const double* Jh);
+/* F = H + 2 J[D] - K[D] for a density D (nbf x nbf, column-major, any
+ * matrix); eelec (may be NULL) receives sum(D .* (H .+ F)) */
+int fcc_scf_build_fock(fcc_scf* s, const double* H, const double* D, double* F, double* eelec);
+/* the same for D = Co Co^T (Co: nbf x nocc occupied coefficients,
+ * RHFa.jl:146-147), with K factored through Co: 4 naux nbf^2 nocc flops
+ * instead of 4 naux nbf^3 */
+int fcc_scf_build_fock_occ(fcc_scf* s, const double* H, const double* Co, int32_t nocc, double* F, double* eelec);
+
 void fcc_destroy(fcc_ctx* ctx);
 const char* fcc_strerror(int code);
 /* Message of the last failing call on this context ("" if none). */

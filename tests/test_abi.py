@@ -71,3 +71,19 @@ def test_no_cpu_fallback_without_gpu(lib):
     from fermicc import _lib
     h = ctypes.c_void_p()
     assert lib.fcc_create(ctypes.byref(h), 5, 19, 84, 0) == _lib.FCC_ERR_NO_DEVICE
+
+
+def test_scf_handle_rejects_bad_arguments_without_device(lib):
+    from fermicc import _lib
+    h = ctypes.c_void_p()
+    assert lib.fcc_scf_create(None, 24, 84, 0) == _lib.FCC_ERR_BAD_ARG
+    assert lib.fcc_scf_create(ctypes.byref(h), 0, 84, 0) == _lib.FCC_ERR_BAD_ARG
+    assert lib.fcc_scf_create(ctypes.byref(h), 24, 0, 0) == _lib.FCC_ERR_BAD_ARG
+    rc = lib.fcc_scf_create(ctypes.byref(h), 24, 84, 0)
+    if rc == 0:                                  # a GB300 is present
+        lib.fcc_scf_destroy(h)
+    else:
+        assert rc == _lib.FCC_ERR_NO_DEVICE and not h.value
+    assert lib.fcc_scf_build_fock(None, None, None, None, None) == _lib.FCC_ERR_BAD_ARG
+    assert lib.fcc_scf_last_error(None) == b""
+    lib.fcc_scf_destroy(None)
