@@ -170,9 +170,11 @@ def df_ao_problem(atoms, keep_pqp: bool = False) -> AOProblem:
                      e_nuc=_nuclear_repulsion(xyz, Z))
 
 
-def df_inputs(atoms, frozen_core: bool = True, keep_ao: bool = False) -> CCInputs:
+def df_inputs(atoms, frozen_core: bool = True, keep_ao: bool = False, rhf_device: bool = False) -> CCInputs:
     """DF-RHF on the stand-in basis, then BOO/BOV/BVV with the core dropped
-    (and, with keep_ao, the AO factors and orbitals for a device MO transform)."""
+    (and, with keep_ao, the AO factors and orbitals for a device MO transform).
+    With rhf_device the RHF is fermicc's RHFcuda (RHFa iterations, Fock build on
+    the GPU) instead of the host SCF below."""
     ao = df_ao_problem(atoms, keep_pqp=keep_ao)
     H, S, b, Jh, ndocc, frozen, e_nuc = ao.H, ao.S, ao.b, ao.Jh, ao.ndocc, ao.frozen, ao.e_nuc
     if not frozen_core:
@@ -189,7 +191,18 @@ def df_inputs(atoms, frozen_core: bool = True, keep_ao: bool = False) -> CCInput
         K = bi2 @ bi2.T
         return J, K
 
-    E, eps, C, nit = _scf(H, S, ndocc, jk, e_nuc)
+    if rhf_device:
+        from ..rhf import RHF, DFFock
+        fock = DFFock(n, naux, b=b)
+        try:
+            r = RHF.compute(H, S, ndocc, e_nuc, fock)
+        finally:
+            fock.close()
+        if not r.converged:
+            raise RuntimeError(f"RHF did not converge in {r.iterations} iterations")
+        E, eps, C, nit = r.energy, r.eps, r.C, r.iterations
+    else:
+        E, eps, C, nit = _scf(H, S, ndocc, jk, e_nuc)
     Co = C[:, frozen:ndocc]
     Cv = C[:, ndocc:]
     bo = (b.reshape(naux * n, n) @ Co).reshape(naux, n, -1)           # [Q, mu, i]
@@ -239,12 +252,13 @@ def conv_inputs(atoms, frozen_core: bool = False) -> CCInputs:
                     meta=dict(nbf=n, ndocc=ndocc, frozen=frozen, scf_iters=nit, kind="conv"))
 
 
-def water_inputs(n: int, seed: int = 0, df: bool = True, keep_ao: bool = False) -> CCInputs:
+def water_inputs(n: int, seed: int = 0, df: bool = True, keep_ao: bool = False,
+                 rhf_device: bool = False) -> CCInputs:
     """The workloads: n = 1 (README water, conventional, no frozen core) or a
     seeded (H2O)n cluster with DF and one frozen core orbital per oxygen."""
     atoms = waters(n, seed)
     if df:
-        out = df_inputs(atoms, frozen_core=(n > 1), keep_ao=keep_ao)
+        out = df_inputs(atoms, frozen_core=(n > 1), keep_ao=keep_ao, rhf_device=rhf_device)
     else:
         out = conv_inputs(atoms, frozen_core=False)
     out.meta.update(waters=n, seed=seed)

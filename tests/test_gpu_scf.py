@@ -93,3 +93,20 @@ def test_scf_errors_are_reported():
     F, _ = f.build(p.H, np.zeros((nbf, nbf)))           # still usable after the errors
     assert np.array_equal(F, p.H)
     f.close()
+
+
+def test_pipeline_with_the_device_rhf_gives_the_same_ccsd():
+    # RHF (device Fock build) -> MO factors -> CCSD, against the host SCF
+    from fermicc import Options, RCCSD
+    from fermicc.inputs import scf
+    host = scf.water_inputs(2, seed=0)
+    dev = scf.water_inputs(2, seed=0, rhf_device=True)
+    assert abs(dev.e_ref - host.e_ref) < 1e-9
+    assert np.abs(dev.eps_o - host.eps_o).max() < 1e-7
+    Options.reset()
+    Options.set("cc_max_rms", 1e-9)
+    a = RCCSD.compute(host)
+    b = RCCSD.compute(dev)
+    assert a.converged and b.converged
+    assert abs(a.correlation - b.correlation) < 1e-9
+    Options.reset()
