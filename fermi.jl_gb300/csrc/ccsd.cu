@@ -865,12 +865,15 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
       TcScope scope(kind == K_F64 ? nullptr : &c->tc);
       c->tc.enabled = kind != K_F64;
       c->tc.exact = kind == K_EXACT;
-      // exact-slice width: 7 weight groups (21 slice pairs; their noise floor
-      // in the Jacobi step is ~1e-10 at (H2O)8) while the step is above
-      // max_rms, then 8 groups (28 pairs) to the end.  (6 groups floor at
-      // ~1e-8.)  The width only grows, so the phase cannot cycle.
+      // exact-slice width by the size of the step: 6 weight groups (15 slice
+      // pairs; noise floor in the Jacobi step ~1e-8 at (H2O)8) while the step
+      // is above 100 max_rms, 7 groups (21 pairs, floor ~1e-10) while it is
+      // above max_rms, then 8 groups (28 pairs) to the end.  The width only
+      // grows, so the phase cannot cycle.
       if (kind == K_EXACT) {
-        const int groups = (exact_groups == OZ_G_DEFAULT || rms < op.max_rms) ? OZ_G_DEFAULT : OZ_G_DEFAULT - 1;
+        const int want = rms < op.max_rms ? OZ_G_DEFAULT
+                                          : (rms < 100.0 * op.max_rms ? OZ_G_DEFAULT - 1 : OZ_G_DEFAULT - 2);
+        const int groups = std::max(exact_groups, want);
         if (groups != exact_groups) { best_rms = 1e300; stalled = 0; }
         exact_groups = groups;
         c->tc.oz_groups = groups;

@@ -88,3 +88,40 @@ extern "C" int fcc_test_contract(int32_t precision, const char* spec, const doub
     return FCC_ERR_CUDA;
   }
 }
+
+extern "C" int fcc_test_split3(const double* x, int64_t R, int64_t K, int32_t row_fastest, double scale,
+                               uint16_t* out) {
+  try {
+    if (!x || !out || R < 1 || K < 1) return FCC_ERR_BAD_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return FCC_ERR_NO_DEVICE;
+    FCC_CUDA(cudaSetDevice(0));
+    cudaStream_t s;
+    FCC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    struct SDel { cudaStream_t s; ~SDel() { cudaStreamDestroy(s); } } sdel{s};
+    // source R x K, row-major (k fastest) or column-major (r fastest); three
+    // planes hi | mid | lo per packed row
+    fcc::PackSpec ps;
+    ps.R = R;
+    ps.K = K;
+    ps.P = 3;
+    ps.Kp = 3 * K;
+    ps.code = 0u | (1u << 2) | (2u << 4);
+    ps.scale = scale;
+    ps.rd2 = 1; ps.rd3 = R; ps.rs1 = 0; ps.rs2 = 0; ps.rs3 = row_fastest ? 1 : K;
+    ps.kd2 = 1; ps.kd3 = K; ps.ks1 = 0; ps.ks2 = 0; ps.ks3 = row_fastest ? R : 1;
+    fcc::DBuf<double> dx;
+    fcc::DBuf<__nv_bfloat16> dy;
+    dx.alloc(R * K);
+    dy.alloc(R * 3 * K);
+    FCC_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * R * K, cudaMemcpyHostToDevice, s));
+    fcc::pack_split(dx.p, ps, dy.p, s);
+    FCC_CUDA(cudaMemcpyAsync(out, dy.p, sizeof(uint16_t) * R * 3 * K, cudaMemcpyDeviceToHost, s));
+    FCC_CUDA(cudaStreamSynchronize(s));
+    return FCC_OK;
+  } catch (const fcc::Error& e) {
+    return e.code;
+  } catch (...) {
+    return FCC_ERR_CUDA;
+  }
+}

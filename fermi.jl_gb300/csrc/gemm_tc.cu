@@ -41,12 +41,78 @@ struct TcCfg {
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024;  // + alignment slack
 };
 
-// hi, mid, lo bf16 pieces of x (x - hi - mid - lo ~ 2^-25 |x|)
+// bf16 bits of (-1)^sgn * m * 2^e for 0 <= m <= 256; zero below the bf16
+// normal range (|value| < 2^-126), infinity above it.
+__device__ __forceinline__ uint16_t bf16_bits(uint32_t sgn, uint32_t m, int e) {
+  if (m == 0) return 0;
+  const int lz = __clz(m) - 24;              // m in [1, 255]: shift up to [128, 255]
+  if (lz >= 0) { m <<= lz; e -= lz; }
+  else { m >>= 1; e += 1; }                  // m == 256
+  const int b = e + 7 + 127;                 // m * 2^e = (m / 128) * 2^(e + 7)
+  if (b <= 0) return 0;
+  if (b >= 255) return (uint16_t)((sgn << 15) | 0x7F80u);
+  return (uint16_t)((sgn << 15) | ((uint32_t)b << 7) | (m & 0x7Fu));
+}
+
+// a (0 < a < 2^62) rounded to nearest-even at 8 significant bits: returns m
+// in [1, 256] with a ~ m * 2^sh
+__device__ __forceinline__ uint32_t round8(uint64_t a, int& sh) {
+  const int n = 64 - __clzll((long long)a);
+  if (n <= 8) { sh = 0; return (uint32_t)a; }
+  sh = n - 8;
+  const uint64_t q = a >> sh, rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+  return (uint32_t)(q + ((rem > half || (rem == half && (q & 1))) ? 1u : 0u));
+}
+
+// hi, mid, lo bf16 pieces of x, each the nearest (ties to even) 8-bit value to
+// what the previous pieces leave, so |x - hi - mid - lo| <= 2^-24 |x|
+// (typically ~2^-27; pieces below the bf16 range become zero).  Integer arithmetic on the
+// FP64 bit pattern: the remainders are exact and no FP64 instruction (a slow
+// pipe on this part) is issued.
 __device__ __forceinline__ void split3(double x, __nv_bfloat16 (&lv)[3]) {
-  lv[0] = __float2bfloat16_rn((float)x);
-  const double r = x - (double)__bfloat162float(lv[0]);
-  lv[1] = __float2bfloat16_rn((float)r);
-  lv[2] = __float2bfloat16_rn((float)(r - (double)__bfloat162float(lv[1])));
+  const uint64_t u = (uint64_t)__double_as_longlong(x);
+  const int ex = (int)((u >> 52) & 0x7FF);
+  uint16_t h = 0, m = 0, l = 0;
+  if (ex == 0x7FF) {                         // inf / nan
+    lv[0] = __float2bfloat16_rn((float)x);
+    lv[1] = lv[2] = __ushort_as_bfloat16((unsigned short)0);
+    return;
+  }
+  if (ex != 0) {                             // zero and FP64 subnormals give zeros
+    const uint64_t M = (u & ((1ull << 52) - 1)) | (1ull << 52);   // |x| = M 2^e0
+    const int e0 = ex - 1075;
+    uint32_t sg = (uint32_t)(u >> 63);
+    int sh;
+    uint32_t q = round8(M, sh);
+    h = bf16_bits(sg, q, e0 + sh);
+    int64_t r = (int64_t)M - ((int64_t)q << sh);
+    if (r != 0) {
+      if (r < 0) { sg ^= 1u; r = -r; }
+      q = round8((uint64_t)r, sh);
+      m = bf16_bits(sg, q, e0 + sh);
+      r -= (int64_t)q << sh;
+      if (r != 0) {
+        if (r < 0) { sg ^= 1u; r = -r; }
+        q = round8((uint64_t)r, sh);
+        l = bf16_bits(sg, q, e0 + sh);
+      }
+    }
+  }
+  lv[0] = __ushort_as_bfloat16(h);
+  lv[1] = __ushort_as_bfloat16(m);
+  lv[2] = __ushort_as_bfloat16(l);
+}
+
+// piece `lev` (0 hi, 1 mid, 2 lo) without a dynamically indexed local array
+__device__ __forceinline__ __nv_bfloat16 piece(const __nv_bfloat16 (&lv)[3], int lev) {
+  return lev == 0 ? lv[0] : (lev == 1 ? lv[1] : lv[2]);
+}
+
+// v * scale, with the common scales +-1 as a sign flip on the bit pattern
+__device__ __forceinline__ double scaled(double v, double scale) {
+  if (scale == 1.0) return v;
+  if (scale == -1.0) return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
+  return v * scale;
 }
 
 template <int BN>
@@ -234,7 +300,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             __nv_bfloat16* dst = static_cast<__nv_bfloat16*>(ep.C) + off;
             __nv_bfloat16 lv[3];
             split3(val, lv);
-            for (int p = 0; p < ep.P; ++p) dst[p * ep.piece] = lv[(ep.code >> (2 * p)) & 3];
+            for (int p = 0; p < ep.P; ++p) dst[p * ep.piece] = piece(lv, (ep.code >> (2 * p)) & 3);
           } else if (ep.mode == EPI_F32) {
             float* dst = static_cast<float*>(ep.C) + off;
             if (ep.atomic) atomicAdd(dst, (float)val);
@@ -277,21 +343,23 @@ __global__ void pack_rows_kernel(const double* __restrict__ src, PackSpec ps, __
       const int cnt = (int)min((int64_t)4, ps.K - k0);
       PackColIter ci(ps, k0);
       for (int q = 0; q < 4; ++q) {
-        split3(q < cnt ? ps.scale * src[ro + ci.off] : 0.0, lv[q]);
+        split3(q < cnt ? scaled(src[ro + ci.off], ps.scale) : 0.0, lv[q]);
         if (q + 1 < cnt) ci.next(ps);
       }
       for (int p = 0; p < ps.P; ++p) {
         const int lev = (ps.code >> (2 * p)) & 3;
         __nv_bfloat16* d = drow + p * ps.K + k0;
         if (cnt == 4 && (reinterpret_cast<uintptr_t>(d) & 7) == 0) {
-          __nv_bfloat162 v0 = __halves2bfloat162(lv[0][lev], lv[1][lev]);
-          __nv_bfloat162 v1 = __halves2bfloat162(lv[2][lev], lv[3][lev]);
+          __nv_bfloat162 v0 = __halves2bfloat162(piece(lv[0], lev), piece(lv[1], lev));
+          __nv_bfloat162 v1 = __halves2bfloat162(piece(lv[2], lev), piece(lv[3], lev));
           uint2 u;
           u.x = *reinterpret_cast<uint32_t*>(&v0);
           u.y = *reinterpret_cast<uint32_t*>(&v1);
           *reinterpret_cast<uint2*>(d) = u;
         } else {
-          for (int q = 0; q < cnt; ++q) d[q] = lv[q][lev];
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (q < cnt) d[q] = piece(lv[q], lev);
         }
       }
     }
@@ -316,7 +384,7 @@ __global__ void pack_tiles_kernel(const double* __restrict__ src, PackSpec ps, _
     for (int j = 0; j < 4; ++j) {
       const int kk = ty + 8 * j;
       const int64_t r = r0 + tx, k = k0 + kk;
-      tile[kk][tx] = (r < ps.R && k < ps.K) ? ps.scale * src[pack_row_off(ps, r) + pack_col_off(ps, k)] : 0.0;
+      tile[kk][tx] = (r < ps.R && k < ps.K) ? scaled(src[pack_row_off(ps, r) + pack_col_off(ps, k)], ps.scale) : 0.0;
     }
     __syncthreads();
     for (int j = 0; j < 4; ++j) {
@@ -326,7 +394,7 @@ __global__ void pack_tiles_kernel(const double* __restrict__ src, PackSpec ps, _
       __nv_bfloat16 lv[3];
       split3(tile[tx][rr], lv);
       __nv_bfloat16* d = dst + r * ps.Kp + k;
-      for (int p = 0; p < ps.P; ++p) d[p * ps.K] = lv[(ps.code >> (2 * p)) & 3];
+      for (int p = 0; p < ps.P; ++p) d[p * ps.K] = piece(lv, (ps.code >> (2 * p)) & 3);
     }
   }
 }

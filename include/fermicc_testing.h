@@ -25,6 +25,12 @@ int fcc_test_contract(int32_t precision, const char* spec, const double* A, cons
                       const double* B, const int64_t* bdims, int32_t brank, double* C, const int64_t* cdims,
                       int32_t crank, double alpha, double beta);
 
+/* The three-piece BF16 split of the tensor-core operand packing on device 0:
+ * x is R x K (row-major, or column-major when row_fastest != 0), multiplied
+ * by scale; out receives R rows of 3K bf16 bit patterns, [hi(K) | mid(K) |
+ * lo(K)] per row. */
+int fcc_test_split3(const double* x, int64_t R, int64_t K, int32_t row_fastest, double scale, uint16_t* out);
+
 /* Number of kernels this library has launched in the process so far. */
 int64_t fcc_stat_launches(void);
 
