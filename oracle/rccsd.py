@@ -274,9 +274,10 @@ class RCCSDResult:
 
 
 def rccsd(I: dict, eps_o, eps_v, e_ref: float, opts: CCOptions | None = None,
-          T1guess=None, T2guess=None, Bvv=None) -> RCCSDResult:
+          T1guess=None, T2guess=None, Bvv=None, ccd: bool = False) -> RCCSDResult:
     """RCCSDa.jl:92-244.  With ``Bvv`` given the DF ladder is used, otherwise
-    ``I["VVVV"]`` (conventional)."""
+    ``I["VVVV"]`` (conventional).  ``ccd`` holds T1 at zero (the CCD limit,
+    a known-answer check against a spin-orbital CCD; not a Fermi option)."""
     opts = opts or CCOptions()
     D1, D2 = denominators(eps_o, eps_v)
     if T1guess is None or T2guess is None:
@@ -287,6 +288,8 @@ def rccsd(I: dict, eps_o, eps_v, e_ref: float, opts: CCOptions | None = None,
         ladder = lambda t1, t2: ladder_conv(t1, t2, I["VVVV"])
     err_dtype = {"double": np.float64, "single": np.float32}.get(opts.diis_prec, np.float16)
     newT1, newT2 = np.array(T1guess, dtype=np.float64), np.array(T2guess, dtype=np.float64)
+    if ccd:
+        newT1[:] = 0.0
     Ecc = cc_update_energy(newT1, newT2, I["OVOV"])                   # :168
     Eguess = Ecc + e_ref
     dE, rms, ite = 1.0, 1.0, 1
@@ -300,15 +303,19 @@ def rccsd(I: dict, eps_o, eps_v, e_ref: float, opts: CCOptions | None = None,
         T1, T2 = newT1.copy(), newT2.copy()                           # :185-186
         oldE = Ecc
         newT1, newT2 = update_amp(T1, T2, I, D1, D2, ladder)          # :190
+        if ccd:
+            newT1 = np.zeros_like(newT1)
         r1 = float(np.sqrt(np.sum((newT1 - T1) ** 2) / T1.size))      # :193
         r2 = float(np.sqrt(np.sum((newT2 - T2) ** 2) / T2.size))      # :194
         diis = False
         if opts.cc_diis:
-            dm1.push(newT1, newT1 - T1)                               # :200-201
+            if not ccd:                                               # (T1 = 0: no T1 subspace)
+                dm1.push(newT1, newT1 - T1)                           # :200-201
             dm2.push(newT2, newT2 - T2)
             if ite >= opts.diis_start and ite % opts.cc_diis_relax == 0:   # :204
                 newT2 = dm2.extrapolate(add_res=True)                 # :206
-                newT1 = dm1.extrapolate(add_res=True)                 # :207
+                if not ccd:
+                    newT1 = dm1.extrapolate(add_res=True)             # :207
                 diis = True
         dp = opts.cc_damp_ratio
         if dp > 0:                                                    # :213-216

@@ -70,8 +70,9 @@ def spin_orbital(g: np.ndarray, eps: np.ndarray, o: int):
     return anti, eps[sp], 2 * o, N
 
 
-def ccsd(anti, f_diag, no, conv=1e-12, max_iter=200):
-    """Stanton-Gauss CCSD with Jacobi updates and a simple DIIS on (t1, t2)."""
+def ccsd(anti, f_diag, no, conv=1e-12, max_iter=200, ccd=False):
+    """Stanton-Gauss CCSD with Jacobi updates and a simple DIIS on (t1, t2);
+    ``ccd`` keeps t1 at zero (CCD)."""
     N = anti.shape[0]
     o, v = slice(0, no), slice(no, N)
     nv = N - no
@@ -113,6 +114,8 @@ def ccsd(anti, f_diag, no, conv=1e-12, max_iter=200):
         tmp = _e("ma,mbij->ijab", t1, anti[o, v, o, o])
         r2 -= tmp - tmp.transpose(0, 1, 3, 2)
         n1, n2 = r1 / Dia, r2 / Dijab
+        if ccd:
+            n1 = np.zeros_like(n1)
         err = np.concatenate([(n1 - t1).ravel(), (n2 - t2).ravel()])
         vec = np.concatenate([n1.ravel(), n2.ravel()])
         hist_t.append(vec); hist_e.append(err)

@@ -152,3 +152,42 @@ def test_df_mp2_pair_loop_equals_the_mp2_guess_energy():
     T1, T2 = R.mp2_guess(I, D1, D2)
     e_guess = R.cc_update_energy(T1, T2, I["OVOV"])
     assert abs(e_pair - e_guess) < 1e-13
+
+
+def test_ccd_limit_equals_spin_orbital_ccd(water_conv):
+    # T1 held at zero in the closed-shell equations = an independent
+    # spin-orbital CCD on the same integrals
+    I = water_conv.conv
+    opts = R.CCOptions(cc_e_conv=1e-12, cc_max_rms=1e-10)
+    res = R.rccsd(I, water_conv.eps_o, water_conv.eps_v, water_conv.e_ref, opts, ccd=True)
+    assert res.converged and np.abs(res.T1).max() == 0.0
+    g = SO.full_spatial_eri(I, water_conv.o, water_conv.v)
+    anti, f, no, _ = SO.spin_orbital(g, np.concatenate([water_conv.eps_o, water_conv.eps_v]), water_conv.o)
+    E, t1, _ = SO.ccsd(anti, f, no, ccd=True)
+    assert np.abs(t1).max() == 0.0
+    assert abs(E - res.correlation) < 1e-10
+    full = _converge(water_conv, df=False)[1]
+    assert abs(full.correlation - res.correlation) > 1e-6       # singles matter: not a vacuous check
+
+
+def test_rotation_and_translation_invariance():
+    # the README water rotated by a random proper rotation and shifted: the same
+    # RHF, CCSD and (T) energies
+    from fermicc.inputs import molecule, scf
+    w = molecule.waters(1, 0)
+    rng = np.random.default_rng(11)
+    Q, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+    if np.linalg.det(Q) < 0:
+        Q[:, 0] *= -1
+    moved = [(e, Q @ p + np.array([1.3, -0.7, 2.1])) for e, p in w]
+    a = scf.conv_inputs(w)
+    b = scf.conv_inputs(moved)
+    assert abs(a.e_ref - b.e_ref) < 1e-10
+    ra = _converge(a, df=False)[1]
+    rb = _converge(b, df=False)[1]
+    # the SCF stops at |dE| < 1e-10 with the commutator below 1e-7: orbital
+    # noise of that size reaches the correlation energy at ~1e-10
+    assert abs(ra.correlation - rb.correlation) < 1e-9
+    ta = T.triples_ijk(ra.T1, ra.T2, a.conv["OVVV"], a.conv["OOOV"], a.conv["OVOV"], a.eps_o, a.eps_v)
+    tb = T.triples_ijk(rb.T1, rb.T2, b.conv["OVVV"], b.conv["OOOV"], b.conv["OVOV"], b.eps_o, b.eps_v)
+    assert abs(ta - tb) < 1e-10
