@@ -191,3 +191,16 @@ def test_rotation_and_translation_invariance():
     ta = T.triples_ijk(ra.T1, ra.T2, a.conv["OVVV"], a.conv["OOOV"], a.conv["OVOV"], a.eps_o, a.eps_v)
     tb = T.triples_ijk(rb.T1, rb.T2, b.conv["OVVV"], b.conv["OOOV"], b.conv["OVOV"], b.eps_o, b.eps_v)
     assert abs(ta - tb) < 1e-10
+
+
+def test_first_update_from_zero_is_the_mp2_guess(water_conv):
+    # one update_amp! from T1 = T2 = 0 gives T1 = 0 and the MP2 amplitudes of
+    # RCCSDa.jl:53-89, hence the guess energy
+    I = water_conv.conv
+    D1, D2 = R.denominators(water_conv.eps_o, water_conv.eps_v)
+    o, v = water_conv.o, water_conv.v
+    T1, T2 = R.update_amp(np.zeros((o, v)), np.zeros((o, o, v, v)), I, D1, D2,
+                          lambda t1, t2: R.ladder_conv(t1, t2, I["VVVV"]))
+    G1, G2 = R.mp2_guess(I, D1, D2)
+    assert np.abs(T1).max() < 1e-14 and np.abs(T2 - G2).max() < 1e-14
+    assert abs(R.cc_update_energy(T1, T2, I["OVOV"]) - R.cc_update_energy(G1, G2, I["OVOV"])) < 1e-14
