@@ -241,11 +241,6 @@ __global__ void axpby4_kernel(const double* __restrict__ in, double* __restrict_
 
 }  // namespace
 
-int& f64_splitk_ctas() {
-  thread_local int ctas = 2 * 152;
-  return ctas;
-}
-
 void contract_f64_launch(const double* A, const double* B, double* C, const CtrDesc& d, cudaStream_t s) {
   if (d.M <= 0 || d.N <= 0 || d.batch <= 0) return;
   int64_t gm = (d.M + BM - 1) / BM, gn = (d.N + BN - 1) / BN;
@@ -260,10 +255,14 @@ void contract_f64_launch(const double* A, const double* B, double* C, const CtrD
     prof_end(s, pidx, PROF_F64, pflops);
     return;
   }
-  // few output tiles and a long K: split K over CTAs (partials reduced in a
-  // fixed order, so results stay deterministic)
-  if (d.batch == 1 && gm * gn < 152 && d.K >= 32 * BK) {
-    int64_t splits = std::min<int64_t>((f64_splitk_ctas() + gm * gn - 1) / (gm * gn), d.K / (8 * BK));
+  // fewer output tiles than one wave of resident CTAs (96 registers x 128
+  // threads: 5 per SM) and a long K: split K so that about 8 CTAs per SM
+  // share the work (partials reduced in a fixed order, so results stay
+  // deterministic).  Under one wave the FP64 pipe idles on DMMA latency:
+  // 387 CTAs ran at 0.8 TFLOP/s where 1216 reach 1.08.
+  constexpr int64_t WAVE_CTAS = 5 * 152, SPLIT_CTAS = 8 * 152;
+  if (d.batch == 1 && gm * gn < WAVE_CTAS && d.K >= 32 * BK) {
+    int64_t splits = std::min<int64_t>((SPLIT_CTAS + gm * gn - 1) / (gm * gn), d.K / (8 * BK));
     splits = std::max<int64_t>(2, std::min<int64_t>(splits, 1024));
     const int64_t chunk = ((d.K + splits - 1) / splits + BK - 1) / BK * BK;
     splits = (d.K + chunk - 1) / chunk;

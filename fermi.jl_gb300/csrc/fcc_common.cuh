@@ -119,14 +119,6 @@ struct CtrDesc {
 };
 
 void contract_f64_launch(const double* A, const double* B, double* C, const CtrDesc& d, cudaStream_t s);
-// CTAs a K-split FP64 contraction aims for when its output has few tiles
-// (per host thread; default 2 per SM).  SplitKTarget sets it for a scope.
-int& f64_splitk_ctas();
-struct SplitKTarget {
-  int prev;
-  explicit SplitKTarget(int ctas) : prev(f64_splitk_ctas()) { f64_splitk_ctas() = ctas; }
-  ~SplitKTarget() { f64_splitk_ctas() = prev; }
-};
 
 // out[perm] = alpha * in + beta * out over a 4-index box (general strides).
 void tensor_axpby_launch(const TView& in, const TView& out, double alpha, double beta, cudaStream_t s);

@@ -88,9 +88,6 @@ int guarded(fcc_scf* s, Fn&& f) {
       if (e != cudaSuccess) { s->last_error = cudaGetErrorString(e); return FCC_ERR_CUDA; }
     }
     fcc::TcScope fp64_only(nullptr);   // every contraction here runs in FP64
-    // the K contraction has a few output tiles and a long K = (Q, s): split it
-    // over about 8 CTAs per SM
-    fcc::SplitKTarget splitk(8 * 152);
     return f();
   } catch (const fcc::Error& e) {
     if (s) s->last_error = e.what;
