@@ -22,6 +22,11 @@
  *   fcc_triples                    RCCSDpT(ccsd, moints, ::ijk),
  *                                  src/Methods/CoupledCluster/PerturbativeTriples/ijk.jl:20-149
  *   fcc_strerror                   FermiException messages, src/Core/Options.jl:196-199
+ *   fcc_upload_ao_df / _ao3_df     the DF fit and MO transform, AtomicIntegrals.jl:31-40,
+ *                                  src/Core/Integrals/ROIntegrals/DFERI.jl:15-69
+ *   fcc_mp2_energy                 RMP2_energy, src/Methods/MollerPlesset/RMP2/RMP2a.jl:91-140
+ *   fcc_scf_build_fock(_occ)       build_fock! (DF), src/Methods/HartreeFock/RHF/RHFHelper.jl:88-93,
+ *                                  and RHFEnergy, RHFHelper.jl:65-67
  */
 #ifndef FERMICC_H
 #define FERMICC_H

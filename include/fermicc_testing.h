@@ -10,6 +10,8 @@
 
 #include <stdint.h>
 
+#include "fermicc.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -36,7 +38,6 @@ int64_t fcc_stat_launches(void);
 
 /* The CUDA stream (cudaStream_t) every call on ctx runs on, so a caller can
  * bracket library work with its own events. */
-typedef struct fcc_ctx fcc_ctx;
 void* fcc_stream(const fcc_ctx* ctx);
 
 /* Force the B tile width (128, 160, 192, 256; 0 = chosen from v) of the mixed
