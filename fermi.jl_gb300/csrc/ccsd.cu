@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "../../include/fermicc_testing.h"
 #include "fcc_ctx.cuh"
 
 namespace fcc {
@@ -692,11 +693,13 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
   fcc_opts op = *opt;
   if (op.max_iter < 0 || op.ndiis < 1 || op.ndiis > MAX_DIIS || op.diis_relax < 1 || op.damp < 0 || op.damp >= 1)
     fail(FCC_ERR_BAD_ARG, "invalid CC options");
-  if (op.precision != FCC_PREC_FP64 && op.precision != FCC_PREC_MIXED)
-    fail(FCC_ERR_BAD_ARG, "precision must be FCC_PREC_FP64 or FCC_PREC_MIXED");
+  if (op.precision != FCC_PREC_FP64 && op.precision != FCC_PREC_MIXED && op.precision != FCC_PREC_EXACT)
+    fail(FCC_ERR_BAD_ARG, "precision must be FCC_PREC_FP64, FCC_PREC_MIXED or FCC_PREC_EXACT");
   if (op.precision == FCC_PREC_MIXED && !(op.mixed_switch_rms > 0))
     fail(FCC_ERR_BAD_ARG, "mixed_switch_rms must be positive");
-  int phase = op.precision;  // mixed: split-BF16 contractions until the switch, then FP64
+  if (op.mixed_finish != FCC_FINISH_EXACT && op.mixed_finish != FCC_FINISH_FP64)
+    fail(FCC_ERR_BAD_ARG, "mixed_finish must be FCC_FINISH_EXACT or FCC_FINISH_FP64");
+  int phase = op.precision;  // mixed: split-BF16 contractions until the switch, then exact-slice, then the finish
   if (!c->dev_err.p) c->dev_err.alloc(1);
   FCC_CUDA(cudaMemsetAsync(c->dev_err.p, 0, sizeof(int), s));
   c->tc.err = c->dev_err.p;
@@ -845,14 +848,23 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
 
   int status = FCC_OK;
   bool conv_final = false;
-  // Iteration kinds: FP64 residual; split-BF16 residual with three products
-  // (mixed form, first phase); exact-slice BF16 residual (mixed form, second
-  // phase: Ozaki-scheme products whose error, ~1e-11 absolute in the
-  // residual, is far below the convergence criteria).  The mixed form ends
-  // only on an FP64 residual evaluation that meets the criteria, so its
-  // converged amplitudes are the FP64 fixed point.
-  enum { K_F64 = 0, K_MIX = 1, K_EXACT = 2 };
-  int kind = (phase == FCC_PREC_MIXED) ? K_MIX : K_F64;
+  // Iteration kinds: FP64 residual (DMMA); split-BF16 residual with three
+  // products (mixed form, first phase); exact-slice BF16 residual at 6-8
+  // weight groups (mixed form, second phase: Ozaki-scheme products whose
+  // error, ~1e-11 absolute in the residual, is far below the convergence
+  // criteria); exact-slice residual at 9 weight groups, whose truncation
+  // (below 2^-47 of max|A_r| max|B_c| per term) and exact accumulation give
+  // FP64-class contractions.  A run ends only on an iteration of its finish
+  // kind that meets the criteria: FP64 for the FP64 form and for the mixed
+  // form with FCC_FINISH_FP64, the 9-group exact-slice residual for
+  // FCC_PREC_EXACT and for the mixed form with FCC_FINISH_EXACT, so the
+  // converged amplitudes are the fixed point of an FP64-accurate residual.
+  enum { K_F64 = 0, K_MIX = 1, K_EXACT = 2, K_EXACT9 = 3 };
+  constexpr int OZ_G_FINISH = 9;
+  const int finish = (phase == FCC_PREC_FP64) ? K_F64
+                     : (phase == FCC_PREC_EXACT) ? K_EXACT9
+                     : (op.mixed_finish == FCC_FINISH_FP64 ? K_F64 : K_EXACT9);
+  int kind = (phase == FCC_PREC_MIXED) ? K_MIX : finish;
   while (true) {
     if (ite > op.max_iter) { status = FCC_NO_CONVERGE; break; }            // :179-182
     FCC_CUDA(cudaEventRecord(ev0, s));
@@ -864,7 +876,8 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
     {
       TcScope scope(kind == K_F64 ? nullptr : &c->tc);
       c->tc.enabled = kind != K_F64;
-      c->tc.exact = kind == K_EXACT;
+      c->tc.exact = kind == K_EXACT || kind == K_EXACT9;
+      if (kind == K_EXACT9) c->tc.oz_groups = OZ_G_FINISH;
       // exact-slice width by the size of the step: 6 weight groups (15 slice
       // pairs; noise floor in the Jacobi step ~1e-8 at (H2O)8) while the step
       // is above 100 max_rms, 7 groups (21 pairs, floor ~1e-10) while it is
@@ -879,7 +892,17 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
         c->tc.oz_groups = groups;
       }
       c->tc.scheme = SPLIT3;
+      if (c->test_fault == FCC_TEST_FAULT_NO_LOADS && kind == K_MIX) {
+        c->tc.no_loads_once = 1;
+        c->test_fault = 0;
+      }
       residual(c);                                                         // :190
+      if (c->test_fault == FCC_TEST_FAULT_NAN) {
+        const double nan = std::nan("");
+        FCC_CUDA(cudaMemcpyAsync(c->r2.p, &nan, sizeof(double), cudaMemcpyHostToDevice, s));
+        FCC_CUDA(cudaStreamSynchronize(s));
+        c->test_fault = 0;
+      }
     }
     double ss1, ss2, e_dummy, e_new;
     run_update(2, D1s, c->dvec1, c->derr1s, c->derr1d, c->t1.p, c->r1.p, tn1, &cur1, nullptr, &ss1, &e_dummy);
@@ -911,7 +934,7 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
     rms = std::max(r1, r2);                                                // :220
     const double prev_dE = dE;
     dE = Ecc - oldE;                                                       // :221
-    bool converged = iter_kind == K_F64 && std::fabs(dE) < op.e_conv && rms < op.max_rms;   // :178
+    bool converged = iter_kind == finish && std::fabs(dE) < op.e_conv && rms < op.max_rms;   // :178
     if (phase == FCC_PREC_MIXED && !converged) {
       // leave a reduced-precision phase once its residual is below the
       // threshold (split-BF16: mixed_switch_rms; exact-slice: the reference's
@@ -929,7 +952,7 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
         // change is the next step of the same convergence) meets them at once
         const bool tight = rms < 0.1 * op.max_rms && std::fabs(dE) < 0.1 * op.e_conv &&
                            std::fabs(prev_dE) < op.e_conv;
-        if (tight || stalled >= 5) kind = K_F64;
+        if (tight || stalled >= 5) kind = finish;
       }
     }
     FCC_CUDA(cudaEventRecord(ev1, s));

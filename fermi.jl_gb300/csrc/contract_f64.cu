@@ -29,53 +29,35 @@ __device__ __forceinline__ void dmma884(double& d0, double& d1, double a, double
                : "d"(a), "d"(b));
 }
 
-__global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restrict__ A,
-                                                          const double* __restrict__ B,
-                                                          double* __restrict__ C, CtrDesc d,
-                                                          int a_mfast, int b_nfast, int64_t k_chunk,
-                                                          double* __restrict__ partial) {
-  __shared__ double As[BK][LDS];
-  __shared__ double Bs[BK][LDS];
-  __shared__ int64_t rowA[BM], colB[BN];
-  __shared__ int8_t rowOK[BM], colOK[BN];
+// Offsets of a 3-level index x = (x1*D2 + x2)*D3 + x3.
+__device__ __forceinline__ int64_t off3(int64_t x, int64_t D2, int64_t D3, int64_t s1, int64_t s2, int64_t s3) {
+  const int64_t x3 = x % D3, r = x / D3;
+  const int64_t x2 = r % D2, x1 = r / D2;
+  return x1 * s1 + x2 * s2 + x3 * s3;
+}
 
+// The k loop of one 64 x 64 output tile: stage A (BM x BK) and B (BK x BN)
+// into shared memory, then 4 k-steps of m8n8k4 per 16-deep slab.  EDGE tiles
+// (the last row or column tile of a ragged extent) skip the MMAs of 8-wide
+// blocks that lie wholly outside the output, so a v = 152 extent (tiles of
+// 64 + 64 + 24) issues no DMMA work for the 40 missing columns.
+template <bool EDGE>
+__device__ __forceinline__ void f64_mainloop(const double* __restrict__ A, const double* __restrict__ B,
+                                             const CtrDesc& d, int a_mfast, int b_nfast, int64_t kbeg,
+                                             int64_t kend, double (&As)[BK][LDS], double (&Bs)[BK][LDS],
+                                             const int64_t* rowA, const int64_t* colB, const int8_t* rowOK,
+                                             const int8_t* colOK, int64_t m0, int64_t n0,
+                                             double (&acc)[4][4][2]) {
   const int tid = threadIdx.x;
-  const int64_t m0 = (int64_t)blockIdx.x * BM;
-  const int64_t n0 = (int64_t)blockIdx.y * BN;
-  // blockIdx.z: batch index, or the K slice when split over K (partial != 0)
-  const int64_t bz = partial ? 0 : blockIdx.z;
-  const int64_t kbeg = partial ? (int64_t)blockIdx.z * k_chunk : 0;
-  const int64_t kend = partial ? min(d.K, kbeg + k_chunk) : d.K;
-  A += bz * d.a_b;
-  B += bz * d.b_b;
-  C += bz * d.c_b;
-
-  if (tid < BM) {
-    int64_t m = m0 + tid;
-    bool ok = m < d.M;
-    int64_t m1 = ok ? m / d.M2 : 0, m2 = ok ? m - m1 * d.M2 : 0;
-    rowA[tid] = m1 * d.a_m1 + m2 * d.a_m2;
-    rowOK[tid] = ok;
-  } else {
-    int t = tid - BM;
-    int64_t n = n0 + t;
-    bool ok = n < d.N;
-    int64_t n1 = ok ? n / d.N2 : 0, n2 = ok ? n - n1 * d.N2 : 0;
-    colB[t] = n1 * d.b_n1 + n2 * d.b_n2;
-    colOK[t] = ok;
-  }
-  __syncthreads();
-
   const int warp = tid >> 5, lane = tid & 31;
   const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-  double acc[4][4][2];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
-
+  // row (column) blocks of 8 of this warp that lie inside the output
+  int ni = 4, nj = 4;
+  if (EDGE) {
+    ni = (int)max((int64_t)0, min((int64_t)4, (d.M - m0 - wm + 7) / 8));
+    nj = (int)max((int64_t)0, min((int64_t)4, (d.N - n0 - wn + 7) / 8));
+  }
   for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
-    // ---- stage A (BM x BK) and B (BK x BN) into shared memory
     if (a_mfast) {
       int m = tid & 63, kb = tid >> 6;
 #pragma unroll
@@ -133,7 +115,6 @@ __global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restri
       }
     }
     __syncthreads();
-    // ---- 4 k-steps of m8n8k4 per 16-deep tile
 #pragma unroll
     for (int ks = 0; ks < BK; ks += 4) {
       double af[4], bf[4];
@@ -144,31 +125,82 @@ __global__ void __launch_bounds__(NT) contract_f64_kernel(const double* __restri
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) dmma884(acc[i][j][0], acc[i][j][1], af[i], bf[j]);
+        for (int j = 0; j < 4; ++j)
+          if (!EDGE || (i < ni && j < nj)) dmma884(acc[i][j][0], acc[i][j][1], af[i], bf[j]);   // warp-uniform
     }
     __syncthreads();
   }
+}
+
+__global__ void __launch_bounds__(NT, 5) contract_f64_kernel(const double* __restrict__ A,
+                                                          const double* __restrict__ B,
+                                                          double* __restrict__ C, CtrDesc d,
+                                                          int a_mfast, int b_nfast, int64_t k_chunk,
+                                                          double* __restrict__ partial) {
+  __shared__ double As[BK][LDS];
+  __shared__ double Bs[BK][LDS];
+  __shared__ int64_t rowA[BM], colB[BN], rowC[BM], colC[BN];
+  __shared__ int8_t rowOK[BM], colOK[BN];
+
+  const int tid = threadIdx.x;
+  const int64_t m0 = (int64_t)blockIdx.x * BM;
+  const int64_t n0 = (int64_t)blockIdx.y * BN;
+  // blockIdx.z: batch index, or the K slice when split over K (partial != 0)
+  const int64_t bz = partial ? 0 : blockIdx.z;
+  const int64_t kbeg = partial ? (int64_t)blockIdx.z * k_chunk : 0;
+  const int64_t kend = partial ? min(d.K, kbeg + k_chunk) : d.K;
+  A += bz * d.a_b;
+  B += bz * d.b_b;
+  C += bz * d.c_b;
+
+  if (tid < BM) {
+    const int64_t m = m0 + tid;
+    const bool ok = m < d.M;
+    rowA[tid] = ok ? off3(m, d.M2, d.M3, d.a_m1, d.a_m2, d.a_m3) : 0;
+    rowC[tid] = ok ? off3(m, d.M2, d.M3, d.c_m1, d.c_m2, d.c_m3) : 0;
+    rowOK[tid] = ok;
+  } else {
+    const int t = tid - BM;
+    const int64_t n = n0 + t;
+    const bool ok = n < d.N;
+    colB[t] = ok ? off3(n, d.N2, d.N3, d.b_n1, d.b_n2, d.b_n3) : 0;
+    colC[t] = ok ? off3(n, d.N2, d.N3, d.c_n1, d.c_n2, d.c_n3) : 0;
+    colOK[t] = ok;
+  }
+  __syncthreads();
+
+  const int warp = tid >> 5, lane = tid & 31;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  double acc[4][4][2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+
+  if (m0 + BM <= d.M && n0 + BN <= d.N)
+    f64_mainloop<false>(A, B, d, a_mfast, b_nfast, kbeg, kend, As, Bs, rowA, colB, rowOK, colOK, m0, n0, acc);
+  else
+    f64_mainloop<true>(A, B, d, a_mfast, b_nfast, kbeg, kend, As, Bs, rowA, colB, rowOK, colOK, m0, n0, acc);
 
   // ---- epilogue: C = alpha * acc + beta * C with general output strides
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    int ml = wm + 8 * i + (lane >> 2);
-    int64_t m = m0 + ml;
+    const int ml = wm + 8 * i + (lane >> 2);
+    const int64_t m = m0 + ml;
     if (m >= d.M) continue;
-    int64_t m1 = m / d.M2, m2 = m - m1 * d.M2;
-    int64_t crow = m1 * d.c_m1 + m2 * d.c_m2;
+    const int64_t crow = rowC[ml];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        int64_t n = n0 + wn + 8 * j + 2 * (lane & 3) + h;
+        const int nl = wn + 8 * j + 2 * (lane & 3) + h;
+        const int64_t n = n0 + nl;
         if (n >= d.N) continue;
         if (partial) {   // split-K: raw partial sums, reduced in a fixed order later
           partial[((int64_t)blockIdx.z * d.M + m) * d.N + n] = acc[i][j][h];
           continue;
         }
-        int64_t n1 = n / d.N2, n2 = n - n1 * d.N2;
-        double* dst = C + crow + n1 * d.c_n1 + n2 * d.c_n2;
+        double* dst = C + crow + colC[nl];
         double v = d.alpha * acc[i][j][h];
         if (d.beta != 0.0) v += d.beta * *dst;
         *dst = v;
@@ -185,8 +217,7 @@ __global__ void splitk_reduce_kernel(const double* __restrict__ partial, int spl
     double s = 0.0;
     for (int z = 0; z < splits; ++z) s += partial[(int64_t)z * MN + t];
     const int64_t m = t / d.N, n = t - m * d.N;
-    const int64_t m1 = m / d.M2, m2 = m - m1 * d.M2, n1 = n / d.N2, n2 = n - n1 * d.N2;
-    double* dst = C + m1 * d.c_m1 + m2 * d.c_m2 + n1 * d.c_n1 + n2 * d.c_n2;
+    double* dst = C + off3(m, d.M2, d.M3, d.c_m1, d.c_m2, d.c_m3) + off3(n, d.N2, d.N3, d.c_n1, d.c_n2, d.c_n3);
     double v = d.alpha * s;
     if (d.beta != 0.0) v += d.beta * *dst;
     *dst = v;
@@ -204,8 +235,7 @@ __global__ void gemv_f64_kernel(const double* __restrict__ A, const double* __re
   B += bz * d.b_b;
   C += bz * d.c_b;
   for (int64_t m = warp; m < d.M; m += nwarps) {
-    const int64_t m1 = m / d.M2, m2 = m - m1 * d.M2;
-    const double* a = A + m1 * d.a_m1 + m2 * d.a_m2;
+    const double* a = A + off3(m, d.M2, d.M3, d.a_m1, d.a_m2, d.a_m3);
     double s = 0.0;
     for (int64_t k = lane; k < d.K; k += 32) {
       const int64_t k1 = k / d.K2, k2 = k - k1 * d.K2;
@@ -213,7 +243,7 @@ __global__ void gemv_f64_kernel(const double* __restrict__ A, const double* __re
     }
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (lane == 0) {
-      double* dst = C + m1 * d.c_m1 + m2 * d.c_m2;
+      double* dst = C + off3(m, d.M2, d.M3, d.c_m1, d.c_m2, d.c_m3);
       double v = d.alpha * s;
       if (d.beta != 0.0) v += d.beta * *dst;
       *dst = v;
@@ -248,6 +278,9 @@ void contract_f64_launch(const double* A, const double* B, double* C, const CtrD
   if (d.K <= 0) fail(FCC_ERR_BAD_ARG, "empty contraction index");
   const int pidx = prof_begin(s);
   const double pflops = 2.0 * (double)d.M * (double)d.N * (double)d.K * (double)d.batch;
+  // stage along M (N) when the fastest-moving M (N) index has unit stride
+  const int a_fast = (d.M3 > 1 ? d.a_m3 : d.a_m2) == 1 ? 1 : 0;
+  const int b_fast = (d.N3 > 1 ? d.b_n3 : d.b_n2) == 1 ? 1 : 0;
   if (d.N == 1) {
     const int64_t blocks = std::min<int64_t>((d.M + 7) / 8, 152 * 16);
     gemv_f64_kernel<<<dim3((unsigned)blocks, (unsigned)d.batch), 256, 0, s>>>(A, B, C, d);
@@ -266,11 +299,14 @@ void contract_f64_launch(const double* A, const double* B, double* C, const CtrD
     splits = std::max<int64_t>(2, std::min<int64_t>(splits, 1024));
     const int64_t chunk = ((d.K + splits - 1) / splits + BK - 1) / BK * BK;
     splits = (d.K + chunk - 1) / chunk;
-    static thread_local DBuf<double> scratch;
+    DBuf<double> local;
+    DBuf<double>* ws = f64_workspace();
+    if (!ws) ws = &local;
+    DBuf<double>& scratch = *ws;
     const int64_t need = splits * d.M * d.N;
     if ((int64_t)scratch.n < need) scratch.alloc(need);
     dim3 grid((unsigned)gm, (unsigned)gn, (unsigned)splits);
-    contract_f64_kernel<<<grid, NT, 0, s>>>(A, B, C, d, d.a_m2 == 1 ? 1 : 0, d.b_n2 == 1 ? 1 : 0, chunk, scratch.p);
+    contract_f64_kernel<<<grid, NT, 0, s>>>(A, B, C, d, a_fast, b_fast, chunk, scratch.p);
     FCC_CHECK_LAUNCH();
     const int64_t MN = d.M * d.N;
     splitk_reduce_kernel<<<(unsigned)std::min<int64_t>((MN + 255) / 256, 152 * 8), 256, 0, s>>>(scratch.p, (int)splits,
@@ -280,7 +316,7 @@ void contract_f64_launch(const double* A, const double* B, double* C, const CtrD
     return;
   }
   dim3 grid((unsigned)gm, (unsigned)gn, (unsigned)d.batch);
-  contract_f64_kernel<<<grid, NT, 0, s>>>(A, B, C, d, d.a_m2 == 1 ? 1 : 0, d.b_n2 == 1 ? 1 : 0, d.K, nullptr);
+  contract_f64_kernel<<<grid, NT, 0, s>>>(A, B, C, d, a_fast, b_fast, d.K, nullptr);
   FCC_CHECK_LAUNCH();
   prof_end(s, pidx, PROF_F64, pflops);
 }
@@ -421,6 +457,8 @@ void run_tc(TcEngine* tc, double alpha, const TView& A, const TView& B, double b
   ep.nd2 = gn[1].dim; ep.nd3 = gn[2].dim; ep.ns1 = gn[0].s[2]; ep.ns2 = gn[1].s[2]; ep.ns3 = gn[2].s[2];
   ep.alpha = alpha; ep.beta = beta; ep.C = C.p; ep.mode = EPI_F64;
   ep.work = 2.0 * (double)M * (double)N * (double)K * sc.P;
+  ep.no_loads = tc->no_loads_once;
+  tc->no_loads_once = 0;
   gemm_bf16x3(tc->bufA.p, M, 0, tc->bufB.p, N, 0, Kp, ep, tc->err, s);
   tc->tc_calls++;
   tc->tc_flops += 2.0 * (double)M * (double)N * (double)K * sc.P;
@@ -435,6 +473,11 @@ int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 TcEngine*& tc_engine() {
   thread_local TcEngine* e = nullptr;
   return e;
+}
+
+DBuf<double>*& f64_workspace() {
+  thread_local DBuf<double>* w = nullptr;
+  return w;
 }
 
 void einsum(double alpha, const char* spec, const TView& A, const TView& B, double beta, const TView& C,
@@ -475,30 +518,34 @@ void einsum(double alpha, const char* spec, const TView& A, const TView& B, doub
     }
   }
   fuse(gb, 1, spec);
-  fuse(gm, 2, spec);
-  fuse(gn, 2, spec);
+  fuse(gm, 3, spec);
+  fuse(gn, 3, spec);
   fuse(gk, 2, spec);
   if (tc) {
     tc->f64_calls++;
     tc->f64_flops += 2.0 * (double)gdim(gm) * (double)gdim(gn) * (double)gdim(gk) * (double)gdim(gb);
   }
-  // order pairs so the faster-moving member (second) has the smallest stride
-  auto order = [](std::vector<Ix>& g, int op) {
-    if (g.size() == 2 && std::llabs(g[0].s[op]) < std::llabs(g[1].s[op])) std::swap(g[0], g[1]);
-    while (g.size() < 2) g.insert(g.begin(), Ix{1, {0, 0, 0}});
+  // order each group slowest first (the last member has the smallest stride
+  // in the operand read along it), padded at the front with unit indices
+  auto order = [](std::vector<Ix>& g, int op, size_t levels) {
+    std::stable_sort(g.begin(), g.end(), [op](const Ix& a, const Ix& b) { return std::llabs(a.s[op]) > std::llabs(b.s[op]); });
+    while (g.size() < levels) g.insert(g.begin(), Ix{1, {0, 0, 0}});
   };
-  order(gm, 0);
-  order(gn, 1);
-  order(gk, 0);
+  order(gm, 0, 3);
+  order(gn, 1, 3);
+  order(gk, 0, 2);
   if (gb.empty()) gb.push_back(Ix{1, {0, 0, 0}});
   CtrDesc d;
-  d.M = gm[0].dim * gm[1].dim; d.M2 = gm[1].dim;
-  d.N = gn[0].dim * gn[1].dim; d.N2 = gn[1].dim;
+  d.M = gdim(gm); d.M2 = gm[1].dim; d.M3 = gm[2].dim;
+  d.N = gdim(gn); d.N2 = gn[1].dim; d.N3 = gn[2].dim;
   d.K = gk[0].dim * gk[1].dim; d.K2 = gk[1].dim;
   d.batch = gb[0].dim;
-  d.a_m1 = gm[0].s[0]; d.a_m2 = gm[1].s[0]; d.a_k1 = gk[0].s[0]; d.a_k2 = gk[1].s[0]; d.a_b = gb[0].s[0];
-  d.b_k1 = gk[0].s[1]; d.b_k2 = gk[1].s[1]; d.b_n1 = gn[0].s[1]; d.b_n2 = gn[1].s[1]; d.b_b = gb[0].s[1];
-  d.c_m1 = gm[0].s[2]; d.c_m2 = gm[1].s[2]; d.c_n1 = gn[0].s[2]; d.c_n2 = gn[1].s[2]; d.c_b = gb[0].s[2];
+  d.a_m1 = gm[0].s[0]; d.a_m2 = gm[1].s[0]; d.a_m3 = gm[2].s[0];
+  d.a_k1 = gk[0].s[0]; d.a_k2 = gk[1].s[0]; d.a_b = gb[0].s[0];
+  d.b_k1 = gk[0].s[1]; d.b_k2 = gk[1].s[1];
+  d.b_n1 = gn[0].s[1]; d.b_n2 = gn[1].s[1]; d.b_n3 = gn[2].s[1]; d.b_b = gb[0].s[1];
+  d.c_m1 = gm[0].s[2]; d.c_m2 = gm[1].s[2]; d.c_m3 = gm[2].s[2];
+  d.c_n1 = gn[0].s[2]; d.c_n2 = gn[1].s[2]; d.c_n3 = gn[2].s[2]; d.c_b = gb[0].s[2];
   d.alpha = alpha;
   d.beta = beta;
   contract_f64_launch(A.p, B.p, C.p, d, s);
@@ -530,12 +577,12 @@ void einsum1(double alpha, const char* spec, const TView& A, double beta, const 
 
 // ===================================================== allocation-free GEMM
 // fcc_gemm_f64_noalloc: the split-K FP64 (DMMA) contraction for callers that
-// must not allocate device memory -- code that runs while a CUDA graph is
-// being captured, inside a host framework that owns every device allocation
-// through its own pool, or on a latency-critical path where cudaMalloc's
-// implicit synchronisation is not acceptable.  Such callers pass their own
-// device inputs and output; the partial sums of the K slices live in the
-// fixed file-scope array below instead of a cudaMalloc'd buffer.
+// cannot allocate device memory: a host framework that owns every device
+// allocation through its own pool and forbids others, or a latency-critical
+// path where cudaMalloc's implicit device synchronisation is not acceptable.
+// Such callers pass their own device inputs and output; the partial sums of
+// the K slices live in the fixed file-scope array below instead of a
+// cudaMalloc'd buffer.
 //
 // The array holds FCC_NOALLOC_SCRATCH doubles (16 MiB) and stays resident on
 // every GPU that loads this library until the process exits.  Every call
@@ -571,11 +618,19 @@ extern "C" int fcc_gemm_f64_noalloc(int64_t M, int64_t N, int64_t K, double alph
                                     const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* stream) {
   using namespace fcc;
   if (M <= 0 || N <= 0 || K <= 0 || !A || !B || !C || lda < K || ldb < N || ldc < N) return FCC_ERR_BAD_ARG;
+  // M and N are bounded one at a time first, so M * N cannot overflow
+  if (M > FCC_NOALLOC_SCRATCH / 2 || N > FCC_NOALLOC_SCRATCH / 2) return FCC_ERR_BAD_ARG;
   if (M * N > FCC_NOALLOC_SCRATCH / 2) return FCC_ERR_BAD_ARG;   // at least two K slices must fit
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the scratch address is the current device's: the stream must belong to it
+  if (s) {
+    int cur = -1, sdev = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cudaStreamGetDevice(s, &sdev) != cudaSuccess) return FCC_ERR_CUDA;
+    if (cur != sdev) return FCC_ERR_BAD_ARG;
+  }
   int st = FCC_OK;
   double* scratch = noalloc_scratch_ptr(st);
   if (!scratch) return st;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   CtrDesc d;
   d.M = M; d.M2 = 1; d.N = N; d.N2 = N; d.K = K; d.K2 = K; d.batch = 1;
   d.a_m1 = lda; d.a_m2 = 0; d.a_k1 = 0; d.a_k2 = 1; d.a_b = 0;

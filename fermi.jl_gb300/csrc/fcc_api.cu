@@ -22,6 +22,7 @@ int guarded(fcc_ctx* c, F&& f) {
       cudaError_t e = cudaSetDevice(c->device);
       if (e != cudaSuccess) { c->last_error = cudaGetErrorString(e); return FCC_ERR_CUDA; }
     }
+    fcc::WorkspaceScope ws(c ? &c->f64ws : nullptr);
     return f();
   } catch (const fcc::Error& e) {
     if (c) c->last_error = e.what;
@@ -376,7 +377,8 @@ int fcc_triples(fcc_ctx* c, int32_t precision, double* et_out) {
   return guarded(c, [&]() {
     if (!et_out) fcc::fail(FCC_ERR_BAD_ARG, "null output");
     if (!c->have_ccsd) fcc::fail(FCC_ERR_STATE, "run CCSD before (T)");
-    if (precision != FCC_PREC_FP64 && precision != FCC_PREC_MIXED) fcc::fail(FCC_ERR_BAD_ARG, "bad precision");
+    if (precision != FCC_PREC_FP64 && precision != FCC_PREC_MIXED)
+      fcc::fail(FCC_ERR_BAD_ARG, "(T) precision must be FCC_PREC_FP64 or FCC_PREC_MIXED");
     *et_out = precision == FCC_PREC_FP64 ? fcc::triples_fp64(c) : fcc::triples_mixed(c);
     return std::isfinite(*et_out) ? FCC_OK : FCC_ERR_NAN;
   });

@@ -69,6 +69,21 @@ struct DBuf {
   }
 };
 
+// Split-K partial sums of the FP64 contraction go to a buffer owned by the
+// context (or DF-RHF handle) whose call runs on this host thread, so two
+// contexts never share one: contexts may sit on different devices or
+// streams.  Entry points install their buffer with WorkspaceScope; without
+// one, contract_f64_launch allocates a buffer for the call and frees it
+// before returning (cudaFree waits for the device).
+DBuf<double>*& f64_workspace();
+struct WorkspaceScope {
+  DBuf<double>* prev;
+  explicit WorkspaceScope(DBuf<double>* w) : prev(f64_workspace()) { f64_workspace() = w; }
+  ~WorkspaceScope() { f64_workspace() = prev; }
+  WorkspaceScope(const WorkspaceScope&) = delete;
+  WorkspaceScope& operator=(const WorkspaceScope&) = delete;
+};
+
 // A strided view of a device tensor with up to 4 named indices.
 struct TView {
   double* p = nullptr;
@@ -107,15 +122,18 @@ inline TView slice(TView t, int idx, int64_t begin, int64_t count) {
 }
 
 // ---------------------------------------------------------------- kernels
-// Contraction descriptor consumed by the FP64 kernel: M = M1*M2, N = N1*N2,
-// K = K1*K2 with independent strides for every sub-index, plus a batch
-// index with uniform strides.
+// Contraction descriptor consumed by the FP64 kernel: M = M1*M2*M3,
+// N = N1*N2*N3, K = K1*K2 with independent strides for every sub-index
+// (m = (m1*M2 + m2)*M3 + m3, likewise n and k), plus a batch index with
+// uniform strides.  M3 = N3 = 1 with zero strides gives two-level groups.
 struct CtrDesc {
   int64_t M, N, K, M2, N2, K2, batch;
   int64_t a_m1, a_m2, a_k1, a_k2, a_b;
   int64_t b_k1, b_k2, b_n1, b_n2, b_b;
   int64_t c_m1, c_m2, c_n1, c_n2, c_b;
   double alpha, beta;
+  int64_t M3 = 1, N3 = 1;
+  int64_t a_m3 = 0, c_m3 = 0, b_n3 = 0, c_n3 = 0;
 };
 
 void contract_f64_launch(const double* A, const double* B, double* C, const CtrDesc& d, cudaStream_t s);
@@ -125,8 +143,9 @@ void tensor_axpby_launch(const TView& in, const TView& out, double alpha, double
 
 // Einsum front end: C = alpha * contract(A, B) + beta * C.  Subscripts use
 // single letters; every index of C must appear in A or B.  Indices are
-// grouped into batch (A,B,C), M (A,C), N (B,C) and K (A,B); each group may
-// hold at most two indices (batch at most one).
+// grouped into batch (A,B,C), M (A,C), N (B,C) and K (A,B); M and N may hold
+// up to three indices, K two and batch one (after fusing indices that are
+// contiguous in every operand).
 void einsum(double alpha, const char* spec, const TView& A, const TView& B, double beta, const TView& C,
             cudaStream_t s);
 // Single-operand form "abcd->dcba": C = alpha * permute(A) + beta * C.

@@ -36,6 +36,7 @@ struct fcc_ctx {
   fcc::DBuf<double> Tp, Tm, Wp, Wm, LXp, LXm;
   // reductions
   fcc::DBuf<double> red;      // device scratch for scalar reductions
+  fcc::DBuf<double> f64ws;    // split-K partial sums of the FP64 contractions
   int64_t ladder_block = 0;
 
   // DIIS storage (slots of vec + err for T1 and T2)
@@ -53,6 +54,10 @@ struct fcc_ctx {
   std::string ckpt_path;
   int32_t ckpt_every = 0;
   int t3_bn_override = 0;     // test hook: B tile width of the mixed (T) GEMM (0: by v)
+  // test hook, one shot: FCC_TEST_FAULT_NO_LOADS makes the next tensor-core
+  // GEMM of a CCSD run issue no TMA loads (its bounded waits run out);
+  // FCC_TEST_FAULT_NAN writes a NaN into the next doubles residual
+  int test_fault = 0;
 
   // (T) scratch
   fcc::DBuf<double> ovvv, ooov, Wt;
@@ -65,7 +70,9 @@ double cc_energy(fcc_ctx* c, const double* t1, const double* t2);
 double mp2_energy(fcc_ctx* c);
 void residual(fcc_ctx* c);
 int ccsd_run(fcc_ctx* c, const fcc_opts* opts, fcc_iter_stats* log, int32_t log_cap, fcc_ccsd_result* out);
-double triples_fp64(fcc_ctx* c);
+// E(T) in FP64; with `subset`, the energies of those triplets (i >= j >= k)
+// one by one into `each` instead (returns 0)
+double triples_fp64(fcc_ctx* c, const std::vector<int3>* subset = nullptr, std::vector<double>* each = nullptr);
 double triples_mixed(fcc_ctx* c);
 // write amplitudes (device, row-major) to a checkpoint file (checkpoint.cu)
 void checkpoint_write(fcc_ctx* c, const std::string& path, const double* t1, const double* t2, double ecc,

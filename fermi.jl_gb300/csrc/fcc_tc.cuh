@@ -86,6 +86,7 @@ struct EpiMap {
   int P = 3;
   uint32_t code = 0;
   double work = 0.0;   // algorithmic BF16 flops for the timing log (0: use the padded count)
+  int no_loads = 0;    // test hook: the producer issues no TMA loads, so the bounded waits give up
 };
 
 int64_t packed_kp(int64_t K, int P = 3);
@@ -134,6 +135,7 @@ struct TcEngine {
   int64_t min_dim = 16;   // smallest M and N routed to the tensor cores
   DBuf<__nv_bfloat16> bufA, bufB;
   int* err = nullptr;
+  int no_loads_once = 0;   // test hook: the next split-BF16 GEMM runs with EpiMap::no_loads
   int64_t tc_calls = 0, f64_calls = 0;
   double tc_flops = 0, f64_flops = 0;
 };

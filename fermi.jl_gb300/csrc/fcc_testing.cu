@@ -37,6 +37,37 @@ extern "C" int fcc_test_set_t3_bn(fcc_ctx* c, int32_t bn) {
   return FCC_OK;
 }
 
+extern "C" int fcc_test_inject(fcc_ctx* c, int32_t kind) {
+  if (!c || !(kind == 0 || kind == FCC_TEST_FAULT_NO_LOADS || kind == FCC_TEST_FAULT_NAN)) return FCC_ERR_BAD_ARG;
+  c->test_fault = kind;
+  return FCC_OK;
+}
+
+extern "C" int fcc_test_triples_subset(fcc_ctx* c, const int32_t* ijk, int32_t n, double* e_each) {
+  if (!c || !ijk || !e_each || n < 1) return FCC_ERR_BAD_ARG;
+  try {
+    FCC_CUDA(cudaSetDevice(c->device));
+    if (!c->have_ccsd) return FCC_ERR_STATE;
+    std::vector<int3> sub;
+    for (int32_t q = 0; q < n; ++q) {
+      const int i = ijk[3 * q], j = ijk[3 * q + 1], k = ijk[3 * q + 2];
+      if (!(0 <= k && k <= j && j <= i && i < c->o)) return FCC_ERR_BAD_ARG;
+      sub.push_back(make_int3(i, j, k));
+    }
+    std::vector<double> each;
+    fcc::WorkspaceScope ws(&c->f64ws);
+    fcc::TcScope fp64(nullptr);
+    fcc::triples_fp64(c, &sub, &each);
+    for (int32_t q = 0; q < n; ++q) e_each[q] = each[q];
+    return FCC_OK;
+  } catch (const fcc::Error& e) {
+    c->last_error = e.what;
+    return e.code;
+  } catch (...) {
+    return FCC_ERR_CUDA;
+  }
+}
+
 extern "C" int fcc_test_contract(int32_t precision, const char* spec, const double* A, const int64_t* adims,
                                  int32_t arank, const double* B, const int64_t* bdims, int32_t brank, double* C,
                                  const int64_t* cdims, int32_t crank, double alpha, double beta) {
@@ -62,7 +93,7 @@ extern "C" int fcc_test_contract(int32_t precision, const char* spec, const doub
     fcc::TcEngine eng;
     eng.enabled = precision != FCC_PREC_FP64;
     if (precision == 2) eng.scheme = fcc::SPLIT6;
-    if (precision == 3 || (precision >= 12 && precision <= 18)) {
+    if (precision == 3 || (precision >= 12 && precision <= 19)) {
       eng.exact = true;
       eng.oz_groups = precision == 3 ? fcc::OZ_G_DEFAULT : precision - 10;
     } else if (precision < 0 || precision > 3) {

@@ -162,8 +162,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int nkt = max(0, ke - kb);
 
   if (warp == 0 && lane == 0) {
-    // ---------------- TMA producer
-    for (int kt = 0; kt < nkt; ++kt) {
+    // ---------------- TMA producer (none at all under the no_loads test hook:
+    // nothing is then in flight, and the MMA thread's bounded wait gives up)
+    for (int kt = 0; kt < (ep.no_loads ? 0 : nkt); ++kt) {
       const int s = kt % Cfg::STAGES;
       const uint32_t ph = (kt / Cfg::STAGES) & 1;
       if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1)) { atomicExch(&abort_flag, 1); break; }

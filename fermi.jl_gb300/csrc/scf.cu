@@ -35,6 +35,7 @@ struct fcc_scf {
   fcc::DBuf<double> b;                // b[Q, mu, nu], column-major
   fcc::DBuf<double> H, D, F, C, Y;    // nbf^2 matrices, occupied orbitals, K intermediate
   fcc::DBuf<double> gam, gpart, red;
+  fcc::DBuf<double> f64ws;            // split-K partial sums of the FP64 contractions
 };
 
 namespace {
@@ -88,6 +89,7 @@ int guarded(fcc_scf* s, Fn&& f) {
       if (e != cudaSuccess) { s->last_error = cudaGetErrorString(e); return FCC_ERR_CUDA; }
     }
     fcc::TcScope fp64_only(nullptr);   // every contraction here runs in FP64
+    fcc::WorkspaceScope ws(s ? &s->f64ws : nullptr);
     return f();
   } catch (const fcc::Error& e) {
     if (s) s->last_error = e.what;

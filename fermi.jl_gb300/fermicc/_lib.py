@@ -23,6 +23,11 @@ FCC_ERR_STATE = -7
 FCC_ERR_NO_DEVICE = -8
 FCC_PREC_FP64 = 0
 FCC_PREC_MIXED = 1
+FCC_PREC_EXACT = 2
+FCC_FINISH_EXACT = 0
+FCC_FINISH_FP64 = 1
+FCC_TEST_FAULT_NO_LOADS = 1
+FCC_TEST_FAULT_NAN = 2
 
 # every symbol include/fermicc.h declares, and the test hooks of include/fermicc_testing.h
 EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess",
@@ -33,13 +38,13 @@ EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv",
            "fcc_mp2_energy", "fcc_upload_ao_df", "fcc_upload_ao3_df", "fcc_scf_create", "fcc_scf_destroy",
            "fcc_scf_last_error", "fcc_scf_upload_b", "fcc_scf_fit", "fcc_scf_build_fock", "fcc_scf_build_fock_occ")
 TEST_EXPORTS = ("fcc_test_contract", "fcc_stat_launches", "fcc_stream", "fcc_prof_enable", "fcc_prof_read",
-                "fcc_test_set_t3_bn", "fcc_test_split3")
+                "fcc_test_set_t3_bn", "fcc_test_split3", "fcc_test_inject", "fcc_test_triples_subset")
 
 
 class FccOpts(ctypes.Structure):
     _fields_ = [("max_iter", ctypes.c_int32), ("diis", ctypes.c_int32), ("ndiis", ctypes.c_int32),
                 ("diis_start", ctypes.c_int32), ("diis_relax", ctypes.c_int32), ("diis_prec", ctypes.c_int32),
-                ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32), ("e_conv", ctypes.c_double),
+                ("precision", ctypes.c_int32), ("mixed_finish", ctypes.c_int32), ("e_conv", ctypes.c_double),
                 ("max_rms", ctypes.c_double), ("damp", ctypes.c_double), ("mixed_switch_rms", ctypes.c_double)]
 
 
@@ -120,6 +125,10 @@ def load():
     lib.fcc_test_set_t3_bn.restype = ctypes.c_int
     lib.fcc_test_split3.argtypes = [dp, i64, i64, i32, ctypes.c_double, ctypes.POINTER(ctypes.c_uint16)]
     lib.fcc_test_split3.restype = ctypes.c_int
+    lib.fcc_test_inject.argtypes = [vp, i32]
+    lib.fcc_test_inject.restype = ctypes.c_int
+    lib.fcc_test_triples_subset.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), i32, dp]
+    lib.fcc_test_triples_subset.restype = ctypes.c_int
     lib.fcc_stream.argtypes = [vp]
     lib.fcc_stream.restype = ctypes.c_void_p
     lib.fcc_mp2_energy.argtypes = [vp, dp]

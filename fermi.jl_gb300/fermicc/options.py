@@ -12,9 +12,13 @@ keys the coupled-cluster path reads, plus the keys this backend adds:
   Julia ``ijk`` / ``ijk2`` / ``abc``.
 * ``mp2_alg`` -- 3 selects this backend's DF-RMP2 energy (``RMP2cuda``); Fermi's
   1-2 are its Julia ``RMP2a`` / ``RMP2b``.
-* ``cc_gpu_precision`` -- "fp64" or "mixed" (split-BF16 contractions with an
-  FP64 finish).
-* ``cc_gpu_switch_rms`` -- residual at which the mixed form switches to FP64.
+* ``cc_gpu_precision`` -- "fp64", "mixed" (split-BF16 contractions, then
+  exact-slice products, then an FP64-accurate finish) or "exact" (every
+  residual from exact-slice products at 9 weight groups).
+* ``cc_gpu_switch_rms`` -- residual at which the mixed form leaves the
+  split-BF16 products.
+* ``cc_gpu_finish`` -- finish of the mixed form: "exact" (exact-slice products
+  at 9 weight groups, FP64-accurate) or "fp64" (DMMA).
 * ``cc_gpu_guess`` -- "mp2" or "mlp" (learned T2 initialiser).
 * ``pt_gpu_precision`` -- "fp64" or "mixed" for (T).
 * ``cc_gpu_checkpoint`` / ``cc_gpu_checkpoint_every`` -- checkpoint file of the
@@ -51,6 +55,7 @@ DEFAULT = {
     "precision": "double",
     "cc_gpu_precision": "fp64",
     "cc_gpu_switch_rms": 1e-5,
+    "cc_gpu_finish": "exact",
     "cc_gpu_guess": "mp2",
     "pt_gpu_precision": "fp64",
     "cc_gpu_device": 0,

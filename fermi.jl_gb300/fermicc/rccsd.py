@@ -206,10 +206,15 @@ def _opts_from_options() -> _lib.FccOpts:
     o.diis_prec = 32 if prec == "single" else 64
     o.damp = Options.get("cc_damp_ratio")
     p = Options.get("cc_gpu_precision")
-    if p not in ("fp64", "mixed"):
-        raise FermiException(f"cc_gpu_precision must be fp64 or mixed, got {p!r}")
-    o.precision = _lib.FCC_PREC_FP64 if p == "fp64" else _lib.FCC_PREC_MIXED
+    prec = {"fp64": _lib.FCC_PREC_FP64, "mixed": _lib.FCC_PREC_MIXED, "exact": _lib.FCC_PREC_EXACT}
+    if p not in prec:
+        raise FermiException(f"cc_gpu_precision must be fp64, mixed or exact, got {p!r}")
+    o.precision = prec[p]
     o.mixed_switch_rms = Options.get("cc_gpu_switch_rms")
+    fin = Options.get("cc_gpu_finish")
+    if fin not in ("exact", "fp64"):
+        raise FermiException(f"cc_gpu_finish must be exact or fp64, got {fin!r}")
+    o.mixed_finish = _lib.FCC_FINISH_EXACT if fin == "exact" else _lib.FCC_FINISH_FP64
     return o
 
 

@@ -53,10 +53,17 @@ extern "C" {
 #define FCC_PREC_MIXED 1 /* split-BF16 tensor-core contractions (3 products, FP32  */
                          /* accumulate) until rms < mixed_switch_rms, then exact-  */
                          /* slice BF16 products (Ozaki scheme, exact integer       */
-                         /* accumulation) until the criteria hold, then FP64: the  */
-                         /* run ends on an FP64 residual that meets e_conv /       */
-                         /* max_rms (the FP64 fixed point); denominators, update,  */
-                         /* DIIS and energies are FP64 throughout                  */
+                         /* accumulation) until the criteria hold, then the finish */
+                         /* (mixed_finish): the run ends on an FP64-accurate       */
+                         /* residual that meets e_conv / max_rms (the FP64 fixed   */
+                         /* point); denominators, update, DIIS and energies are    */
+                         /* FP64 throughout                                        */
+#define FCC_PREC_EXACT 2 /* every residual from exact-slice products at 9 weight   */
+                         /* groups (FP64-accurate contractions on the tensor cores)*/
+
+/* finish of the mixed form (fcc_opts.mixed_finish) */
+#define FCC_FINISH_EXACT 0 /* exact-slice products at 9 weight groups (default)   */
+#define FCC_FINISH_FP64 1  /* FP64 (DMMA) contractions                             */
 
 typedef struct fcc_ctx fcc_ctx;
 
@@ -68,8 +75,8 @@ typedef struct {
   int32_t diis_start;      /* diis_start     (3)                               */
   int32_t diis_relax;      /* cc_diis_relax  (3)                               */
   int32_t diis_prec;       /* diis_prec: 32 = "single" (default), 64 = "double" */
-  int32_t precision;       /* FCC_PREC_FP64 (default) or FCC_PREC_MIXED        */
-  int32_t reserved;
+  int32_t precision;       /* FCC_PREC_FP64 (default), _MIXED or _EXACT        */
+  int32_t mixed_finish;    /* FCC_FINISH_EXACT (default) or FCC_FINISH_FP64    */
   double e_conv;           /* cc_e_conv      (1e-10)                           */
   double max_rms;          /* cc_max_rms     (1e-10)                           */
   double damp;             /* cc_damp_ratio  (0.0)                             */
@@ -81,7 +88,8 @@ typedef struct {
   int32_t ite;
   int32_t diis;      /* 1 if this iteration extrapolated                */
   int32_t precision; /* residual of this iteration: 0 FP64, 1 split-BF16, */
-                     /* 2 exact-slice BF16 (Ozaki scheme)                */
+                     /* 2 exact-slice BF16 (Ozaki scheme, 6-8 groups),   */
+                     /* 3 exact-slice at 9 groups (FP64-accurate)        */
   int32_t pad;
   double energy;     /* correlation energy after the iteration          */
   double dE;
@@ -206,19 +214,20 @@ int fcc_mlp_guess(fcc_ctx* ctx, const fcc_mlp* m);
 int fcc_mlp_guess_ex(fcc_ctx* ctx, const fcc_mlp* m, double lam, double thresh);
 
 /* C = alpha * A.B + beta * C in FP64 on the DMMA pipe, split over K, for
- * callers that cannot allocate device memory (while capturing a CUDA graph,
- * inside a framework that owns all device memory through its own pool, or on
- * a path where cudaMalloc's implicit synchronisation is not acceptable).
- * This entry point has no counterpart in Fermi.jl.  A (M x K, leading
- * dimension lda), B (K x N, ldb) and C (M x N, ldc) are ROW-MAJOR DEVICE
- * arrays owned by the caller; the work is queued on `stream` (a
- * cudaStream_t, NULL = legacy default stream) and the call returns without
- * synchronising.  It allocates nothing: partial sums go to a fixed 16 MiB
- * device array that every GPU loading the library keeps until exit, so
- * M * N must not exceed 2^20 (FCC_ERR_BAD_ARG otherwise).  The first call on
- * each device looks up that array's device address and should be made before
- * any stream capture.  Calls share the array: calls that overlap on the GPU
- * race and must be ordered by the caller. */
+ * callers that cannot allocate device memory (a framework that owns all
+ * device memory through its own pool, or a path where cudaMalloc's implicit
+ * device synchronisation is not acceptable).  This entry point has no
+ * counterpart in Fermi.jl.  A (M x K, leading dimension lda), B (K x N, ldb)
+ * and C (M x N, ldc) are ROW-MAJOR DEVICE arrays owned by the caller on the
+ * current device; the work is queued on `stream` (a cudaStream_t of the
+ * current device, NULL = legacy default stream; a stream of another device
+ * gives FCC_ERR_BAD_ARG) and the call returns without synchronising.  It
+ * allocates nothing: partial sums go to a fixed 16 MiB device array that
+ * every GPU loading the library keeps until exit, so M * N must not exceed
+ * 2^20 (FCC_ERR_BAD_ARG otherwise).  The first call on each device looks up
+ * that array's device address and should be made before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race and must be
+ * ordered by the caller. */
 int fcc_gemm_f64_noalloc(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
                          const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* stream);
 

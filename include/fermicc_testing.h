@@ -19,8 +19,8 @@ extern "C" {
 /* C = alpha * einsum(spec, A, B) + beta * C on device 0 for row-major host
  * tensors (rank <= 4 each).  precision FCC_PREC_FP64 runs the DMMA kernel;
  * FCC_PREC_MIXED forces the three-product split-BF16 tensor-core kernel,
- * 2 the six-product one, 3 the exact-slice (Ozaki) kernel with 7 weight
- * groups and 10 + G the exact-slice kernel with G groups (2 <= G <= 8)
+ * 2 the six-product one, 3 the exact-slice (Ozaki) kernel with 8 weight
+ * groups and 10 + G the exact-slice kernel with G groups (2 <= G <= 9)
  * (error if the contraction cannot be expressed for it).  Returns an fcc
  * status code. */
 int fcc_test_contract(int32_t precision, const char* spec, const double* A, const int64_t* adims, int32_t arank,
@@ -43,6 +43,23 @@ void* fcc_stream(const fcc_ctx* ctx);
 /* Force the B tile width (128, 160, 192, 256; 0 = chosen from v) of the mixed
  * (T) GEMM, e.g. to run several column tiles on a small system. */
 int fcc_test_set_t3_bn(fcc_ctx* ctx, int32_t bn);
+
+/* One-shot failure injection on ctx for the error-path tests; nothing here
+ * faults the GPU.  FCC_TEST_FAULT_NO_LOADS: the first split-BF16 tensor-core
+ * GEMM of the next mixed-form fcc_ccsd_run issues no TMA loads, so its MMA
+ * thread's bounded mbarrier wait (2 s) gives up with nothing in flight, the
+ * kernel frees its TMEM and returns, and the run reports FCC_ERR_TIMEOUT.
+ * FCC_TEST_FAULT_NAN: a NaN is written into the doubles residual of the next
+ * iteration before the device update, which then reports FCC_ERR_NAN. */
+#define FCC_TEST_FAULT_NO_LOADS 1
+#define FCC_TEST_FAULT_NAN 2
+int fcc_test_inject(fcc_ctx* ctx, int32_t kind);
+
+/* FP64 (T) energy contributions of n single triplets ijk[3q..3q+2] = (i, j, k)
+ * with i >= j >= k (0-based active occupied indices), each including its
+ * weight 2 - d_ij - d_jk, from the current amplitudes (after fcc_ccsd_run);
+ * the sum over all triplets is the FP64 E(T) that fcc_triples returns. */
+int fcc_test_triples_subset(fcc_ctx* ctx, const int32_t* ijk, int32_t n, double* e_each);
 
 /* Opt-in per-class kernel timing with CUDA events on the launching stream:
  * classes 0 FP64 contractions (work = 2MNK flop), 1 tensor-core GEMMs (work =

@@ -120,21 +120,50 @@ def test_errors_surface_as_status_codes():
     ctx.close()
 
 
-@pytest.mark.parametrize("n", [2, 4])
-def test_mixed_form_reaches_the_fp64_fixed_point(n):
+@pytest.mark.parametrize("n,finish", [(2, "exact"), (4, "exact"), (2, "fp64"), (4, "fp64")])
+def test_mixed_form_reaches_the_fp64_fixed_point(n, finish):
     # split-BF16 iterations until rms < 1e-5, exact-slice BF16 iterations
-    # until the criteria hold, then FP64: same converged energy
+    # until the criteria hold, then the finish (exact-slice products at 9
+    # weight groups, or FP64 DMMA): same converged energy as the FP64 form
     inp = inputs(n)
     opt = dict(cc_e_conv=1e-9, cc_max_rms=1e-8)
     e64 = _gpu_run(inp, **opt)
-    mix = _gpu_run(inp, cc_gpu_precision="mixed", **opt)
+    mix = _gpu_run(inp, cc_gpu_precision="mixed", cc_gpu_finish=finish, **opt)
     assert mix.converged
+    last = 3 if finish == "exact" else 0
     precs = [l["precision"] for l in mix.iterations]
-    assert precs[0] == 1 and precs[-1] == 0          # started mixed, finished FP64
-    assert precs == sorted(precs, key=lambda p: (1, 2, 0).index(p))   # phases 1 -> 2 -> 0
+    assert precs[0] == 1 and precs[-1] == last       # started split-BF16, ended on the finish
+    assert precs == sorted(precs, key=lambda p: (1, 2, last).index(p))   # phases 1 -> 2 -> finish
     assert 2 in precs
-    # the exact-slice residual is accurate enough that the FP64 check passes
-    # at once (allow one more FP64 step for an unlucky dE)
-    assert precs.count(0) <= 2, precs
+    # the exact-slice residual is accurate enough that the finish passes at
+    # once (allow one more step for an unlucky dE)
+    assert precs.count(last) <= 2, precs
     assert abs(mix.correlation - e64.correlation) < 1e-7
     assert np.abs(mix.T2 - e64.T2).max() < 1e-6
+
+
+@pytest.mark.parametrize("n", [2, 4])
+def test_exact_finish_is_the_fp64_fixed_point(n):
+    # the 9-group exact-slice residual (the mixed form's finish) at the FP64
+    # form's tightly converged amplitudes: one Jacobi step from them moves
+    # them no more than the FP64 residual's own step does, to 1e-11, so the
+    # two residuals share the fixed point
+    inp = inputs(n)
+    star = _gpu_run(inp, cc_e_conv=1e-13, cc_max_rms=1e-12, cc_max_iter=200)
+    assert star.converged
+    g = (star.T1, star.T2)
+    s64 = _gpu_run(inp, g, cc_max_iter=1, cc_diis=False)
+    s9 = _gpu_run(inp, g, cc_max_iter=1, cc_diis=False, cc_gpu_precision="exact")
+    assert [l["precision"] for l in s9.iterations] == [3]
+    assert np.abs(s64.T2 - star.T2).max() < 1e-11
+    assert np.abs(s9.T2 - s64.T2).max() < 1e-11
+    assert np.abs(s9.T1 - s64.T1).max() < 1e-11
+    assert abs(s9.correlation - s64.correlation) < 1e-11
+    # and whole runs that end on the exact-slice finish land on the FP64
+    # solution within the distance their convergence criteria allow
+    opt = dict(cc_e_conv=1e-12, cc_max_rms=1e-11, cc_max_iter=100)
+    for prec in ("mixed", "exact"):
+        r = _gpu_run(inp, cc_gpu_precision=prec, cc_gpu_finish="exact", **opt)
+        assert r.converged and r.iterations[-1]["precision"] == 3
+        assert np.abs(r.T2 - star.T2).max() < 1e-8
+        assert abs(r.correlation - star.correlation) < 1e-9

@@ -1,11 +1,13 @@
 """The allocation-free FP64 GEMM entry point (fcc_gemm_f64_noalloc).
 
-Callers that cannot allocate device memory -- code recording a CUDA graph, a
-host framework that hands out every device buffer from its own pool, a path
-that must not absorb cudaMalloc's implicit synchronisation -- pass their own
-device arrays; the entry point keeps its split-K partial sums in a fixed
-device array instead of allocating.  Its results must match the regular
-contraction entry point.  This file is collected last on purpose.
+Some callers cannot allocate device memory: a host framework that hands out
+every device buffer from its own pool and forbids other allocations, or a
+latency-critical path that must not absorb cudaMalloc's implicit device
+synchronisation.  They pass their own device arrays; the entry point keeps
+its split-K partial sums in a fixed device array instead of allocating.
+Its results must equal alpha * A @ B + beta * C computed on the host, on
+consecutive calls that share that array.  This file is collected last on
+purpose.
 """
 import ctypes
 
@@ -14,51 +16,56 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-
-def _regular(A, B, C, alpha, beta):
-    """Same product through fcc_test_contract (host arrays, allocates)."""
-    from fermicc import _lib
-    lib = _lib.load()
-    i64 = lambda shape: (ctypes.c_int64 * len(shape))(*shape)
-    dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-    out = np.ascontiguousarray(C.copy())
-    rc = lib.fcc_test_contract(0, b"mk,kn->mn", dp(A), i64(A.shape), 2, dp(B), i64(B.shape), 2, dp(out),
-                               i64(out.shape), 2, alpha, beta)
-    assert rc == 0
-    return out
+# DMMA products against numpy's BLAS: both are FP64 with different summation
+# orders, so they agree to a small multiple of K * 2^-53 relative
+TOL = 1e-12
 
 
-def test_noalloc_gemm_matches_regular_entry_point_twice():
+def _call(lib, M, N, K, alpha, dA, lda, dB, ldb, beta, dC, ldc, stream):
+    return lib.fcc_gemm_f64_noalloc(M, N, K, alpha, ctypes.c_void_p(dA.data_ptr()), lda,
+                                    ctypes.c_void_p(dB.data_ptr()), ldb, beta, ctypes.c_void_p(dC.data_ptr()), ldc,
+                                    ctypes.c_void_p(stream))
+
+
+def test_noalloc_gemm_matches_host_product_on_consecutive_calls():
     import torch
     from fermicc import _lib
     lib = _lib.load()
     rng = np.random.default_rng(11)
-    stream = torch.cuda.current_stream()
-    # two calls in a row on different data: the shared scratch keeps nothing
-    # that the second call could pick up
-    for call, (M, N, K, alpha, beta) in enumerate([(40, 24, 20000, 1.0, 0.0), (96, 70, 9000, -0.7, 0.5)]):
-        A = rng.standard_normal((M, K))
-        B = rng.standard_normal((K, N))
-        C = rng.standard_normal((M, N))
+    stream = torch.cuda.current_stream().cuda_stream
+    # consecutive calls on different data and shapes: the shared scratch keeps
+    # nothing that a later call could pick up; the second and third use padded
+    # leading dimensions (lda > K, ldb > N, ldc > N)
+    cases = [(40, 24, 20000, 1.0, 0.0, 0, 0, 0), (96, 70, 9000, -0.7, 0.5, 5, 3, 7), (33, 129, 4100, 2.0, -1.0, 1, 9, 2)]
+    for call, (M, N, K, alpha, beta, pa, pb, pc) in enumerate(cases):
+        A = rng.standard_normal((M, K + pa))
+        B = rng.standard_normal((K, N + pb))
+        C = rng.standard_normal((M, N + pc))
         dA = torch.from_numpy(A).cuda()
         dB = torch.from_numpy(B).cuda()
         dC = torch.from_numpy(C).cuda()
         torch.cuda.synchronize()
-        rc = lib.fcc_gemm_f64_noalloc(M, N, K, alpha, ctypes.c_void_p(dA.data_ptr()), K,
-                                      ctypes.c_void_p(dB.data_ptr()), N, beta, ctypes.c_void_p(dC.data_ptr()), N,
-                                      ctypes.c_void_p(stream.cuda_stream))
+        rc = _call(lib, M, N, K, alpha, dA, K + pa, dB, N + pb, beta, dC, N + pc, stream)
         assert rc == 0, (call, rc)
         torch.cuda.synchronize()
         got = dC.cpu().numpy()
-        ref = _regular(A, B, C, alpha, beta)
-        assert np.abs(got - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max()), call
+        ref = alpha * (A[:, :K] @ B[:, :N]) + beta * C[:, :N]
+        assert np.abs(got[:, :N] - ref).max() <= TOL * max(1.0, np.abs(ref).max()), call
+        # the padding columns of C are not written
+        assert np.array_equal(got[:, N:], C[:, N:]), call
 
 
 def test_noalloc_gemm_rejects_sizes_beyond_its_scratch():
     from fermicc import _lib
     lib = _lib.load()
     null = ctypes.c_void_p(0)
-    dummy = ctypes.c_void_p(16)   # never dereferenced: the size check comes first
-    assert lib.fcc_gemm_f64_noalloc(2048, 1024, 64, 1.0, dummy, 64, dummy, 1024, 0.0, dummy, 1024, null) == \
-        _lib.FCC_ERR_BAD_ARG
-    assert lib.fcc_gemm_f64_noalloc(0, 4, 4, 1.0, dummy, 4, dummy, 4, 0.0, dummy, 4, null) == _lib.FCC_ERR_BAD_ARG
+    dummy = ctypes.c_void_p(16)   # never dereferenced: the size checks come first
+    f = lib.fcc_gemm_f64_noalloc
+    assert f(2048, 1024, 64, 1.0, dummy, 64, dummy, 1024, 0.0, dummy, 1024, null) == _lib.FCC_ERR_BAD_ARG
+    assert f(0, 4, 4, 1.0, dummy, 4, dummy, 4, 0.0, dummy, 4, null) == _lib.FCC_ERR_BAD_ARG
+    # M * N would wrap around in 64 bits: rejected before the product is formed
+    big = 1 << 43
+    assert f(big, 1 << 21, 4, 1.0, dummy, 4, dummy, 1 << 21, 0.0, dummy, 1 << 21, null) == _lib.FCC_ERR_BAD_ARG
+    assert f(4, big, 4, 1.0, dummy, 4, dummy, big, 0.0, dummy, big, null) == _lib.FCC_ERR_BAD_ARG
+    # leading dimensions shorter than the rows
+    assert f(4, 4, 8, 1.0, dummy, 7, dummy, 4, 0.0, dummy, 4, null) == _lib.FCC_ERR_BAD_ARG
