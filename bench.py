@@ -86,21 +86,41 @@ def parse():
     ap.add_argument("--part", default="cc", choices=["cc", "rhf-fock"],
                     help="rhf-fock: time the DF-RHF Fock build and the RHF iterations instead (own JSON line)")
     ap.add_argument("--profile-case", default=None,
-                    choices=["ccsd-fp64-iter", "ccsd-mixed-iter", "ccsd-exact-iter", "triples-mixed"],
+                    choices=["ccsd-fp64-iter", "ccsd-mixed-iter", "ccsd-exact-iter", "triples-mixed",
+                             "triples-fp64", "solve-mixed"],
                     help="run one piece of the workload once (for ncu captures) and print its timing, no JSON line")
     return ap.parse_args()
 
 
 def profile_case(args, inp):
     """One piece of the workload, for kernel profiling: one FP64, one
-    split-BF16 or one exact-slice CCSD iteration from the MP2 guess, or the
-    mixed (T) on the amplitudes after two mixed iterations."""
+    split-BF16 or one exact-slice CCSD iteration from the MP2 guess; the mixed
+    (T) on the amplitudes after two mixed iterations; the whole FP64 (T) on the
+    amplitudes after one FP64 iteration; or one whole mixed solve from the
+    learned guess, (T) included."""
     from fermicc import Options, RCCSD, RCCSDpT
     from fermicc.rccsd import Context
     Options.reset()
     ctx = Context(inp)
     t0 = time.perf_counter()
-    if args.profile_case.startswith("ccsd"):
+    if args.profile_case == "solve-mixed":
+        from fermicc.mlp import DEFAULT_PARAMS, MLPGuess
+        Options.set("cc_gpu_precision", "mixed")
+        Options.set("pt_gpu_precision", "mixed")
+        Options.set("cc_e_conv", E_CONV)
+        Options.set("cc_max_rms", MAX_RMS)
+        MLPGuess(0, DEFAULT_PARAMS).guess(ctx)
+        r = RCCSD.compute(inp, context=ctx)
+        pt = RCCSDpT.compute(r, inp)
+        print(json.dumps({"case": args.profile_case, "wall_s": time.perf_counter() - t0, "e_total": pt.energy,
+                          "kinds": [l["precision"] for l in r.iterations]}))
+    elif args.profile_case == "triples-fp64":
+        Options.set("cc_max_iter", 1)
+        r = RCCSD.compute(inp, context=ctx)
+        t0 = time.perf_counter()
+        pt = RCCSDpT.compute(r, inp)
+        print(json.dumps({"case": args.profile_case, "triples_s": time.perf_counter() - t0, "e_t": pt.correction}))
+    elif args.profile_case.startswith("ccsd"):
         Options.set("cc_gpu_precision", "fp64" if "fp64" in args.profile_case else "mixed")
         Options.set("cc_max_iter", 1)
         if "exact" in args.profile_case:
@@ -447,7 +467,7 @@ def main():
     f_it, f_t = algorithmic_flops(inp.o, inp.v, inp.naux)
     # per-class kernel timing over the profiled step (CUDA events on the
     # library's stream): launches, ms, algorithmic work, longest launch
-    cls = {0: "contract_f64_kernel (DMMA FP64)", 1: "gemm_bf16_tc_kernel (tcgen05 split-BF16)",
+    cls = {0: "contract_f64_kernel (DMMA FP64)", 1: "gemm_bf16_tc_kernel + gemm_t3_kernel (tcgen05 split-BF16)",
            2: "pack kernels (split + gather)", 5: "gemm_oz_kernel (tcgen05 exact-slice BF16)"}
     bf = peaks["bf16_tflops_sustained"]
     pk = {0: (FP64_PEAK_TFLOPS, "TFLOP/s"), 1: (bf, "TFLOP/s"), 2: (peaks["hbm_gbs"], "GB/s"), 5: (bf, "TFLOP/s")}

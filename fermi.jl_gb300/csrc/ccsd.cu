@@ -947,12 +947,18 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
         best_rms = 1e300;
         stalled = 0;
       } else if (iter_kind == K_EXACT) {
-        // ten times inside the criteria on this iteration and inside them on
+        // FP64 finish (one DMMA residual costs ~25 exact-slice ones): switch
+        // when the criteria hold ten times over on this iteration and hold on
         // the previous one, so that the FP64 step that follows (whose energy
-        // change is the next step of the same convergence) meets them at once
-        const bool tight = rms < 0.1 * op.max_rms && std::fabs(dE) < 0.1 * op.e_conv &&
-                           std::fabs(prev_dE) < op.e_conv;
-        if (tight || stalled >= 5) kind = finish;
+        // change is the next step of the same convergence) meets them at
+        // once.  Exact-slice finish (about the cost of one more exact-slice
+        // iteration): switch as soon as the criteria hold; a finish step that
+        // misses them is followed by another.
+        const bool ready = finish == K_F64
+                               ? (rms < 0.1 * op.max_rms && std::fabs(dE) < 0.1 * op.e_conv &&
+                                  std::fabs(prev_dE) < op.e_conv)
+                               : (rms < op.max_rms && std::fabs(dE) < op.e_conv);
+        if (ready || stalled >= 5) kind = finish;
       }
     }
     FCC_CUDA(cudaEventRecord(ev1, s));
