@@ -5,8 +5,10 @@
 // converged energy is unaffected.
 //
 // Weights are BF16 for the forward/backward products with FP32 master copies
-// updated by Adam.  Everything here is hand-written: the feature kernel, an
-// FP32 SIMT GEMM (BF16 or FP32 operands), bias+GELU forward and backward,
+// updated by Adam.  Everything here is hand-written: the feature kernel, a
+// BF16 tensor-core GEMM (mma.sync m16n8k16, FP32 accumulation, deterministic
+// split-K) for the five layer products, an FP32 SIMT GEMM for the one-row
+// output-layer gradient, bias+GELU forward and backward,
 // the loss, bias-gradient reductions, Adam, and the inference kernel that
 // writes the guess into a context.
 #include <cuda_bf16.h>
@@ -93,6 +95,135 @@ void sgemm(int M, int N, int K, float alpha, const TA* A, int64_t sam, int64_t s
            int64_t sbn, float beta, float* C, int64_t ldc, cudaStream_t s) {
   dim3 grid((N + 63) / 64, (M + 63) / 64);
   sgemm_kernel<TA, TB><<<grid, 256, 0, s>>>(M, N, K, alpha, A, sam, sak, B, sbk, sbn, beta, C, ldc);
+  FCC_CHECK_LAUNCH();
+}
+
+// ---- tensor-core GEMM of the network's products: operands rounded to BF16
+// (nearest, ties to even) when staged, mma.sync m16n8k16 with FP32
+// accumulation.  64 x 64 output tile, 32-deep K slab, four warps of 32 x 32.
+// With `splits` > 1 the K range is cut into slices whose FP32 partial tiles
+// are summed in slice order by hgemm_reduce_kernel (the gradient products
+// reduce over the whole batch, K = 65536, into a 128 x 128 output).
+constexpr int HT = 64, HK = 32, HLD = HK + 8;   // smem rows padded by 16 bytes
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <class T>
+__device__ __forceinline__ __nv_bfloat16 to_bf(const T* p, int64_t i);
+template <>
+__device__ __forceinline__ __nv_bfloat16 to_bf<float>(const float* p, int64_t i) { return __float2bfloat16_rn(p[i]); }
+template <>
+__device__ __forceinline__ __nv_bfloat16 to_bf<__nv_bfloat16>(const __nv_bfloat16* p, int64_t i) { return p[i]; }
+
+// C[m][n] = alpha * sum_k A(m,k) B(k,n) + beta * C (part == nullptr), or the
+// raw partial of K slice blockIdx.z into part[z][m][n].
+template <class TA, class TB>
+__global__ void __launch_bounds__(128) hgemm_kernel(int M, int N, int K, int kchunk, float alpha,
+                                                    const TA* __restrict__ A, int64_t sam, int64_t sak,
+                                                    const TB* __restrict__ B, int64_t sbk, int64_t sbn, float beta,
+                                                    float* __restrict__ C, int64_t ldc, float* __restrict__ part) {
+  __shared__ __align__(16) __nv_bfloat16 As[HT][HLD];   // [m][k]
+  __shared__ __align__(16) __nv_bfloat16 Bs[HT][HLD];   // [n][k]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * HT, n0 = blockIdx.x * HT;
+  const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int g = lane >> 2, t4 = lane & 3;
+  float acc[2][4][4] = {};
+  for (int k0 = kb; k0 < ke; k0 += HK) {
+    // stage with the stride-1 index of each operand along the threads
+    for (int e = tid; e < HT * HK; e += 128) {
+      const int mm = sak == 1 ? e / HK : e % HT, kk = sak == 1 ? e % HK : e / HT;
+      const int m = m0 + mm, k = k0 + kk;
+      As[mm][kk] = (m < M && k < ke) ? to_bf(A, (int64_t)m * sam + (int64_t)k * sak) : __float2bfloat16_rn(0.0f);
+      const int nn = sbk == 1 ? e / HK : e % HT, k2 = sbk == 1 ? e % HK : e / HT;
+      const int n = n0 + nn, kk2 = k0 + k2;
+      Bs[nn][k2] = (n < N && kk2 < ke) ? to_bf(B, (int64_t)kk2 * sbk + (int64_t)n * sbn) : __float2bfloat16_rn(0.0f);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ks = 0; ks < HK; ks += 16) {
+      uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int r = wm + 16 * i + g;
+        af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 2 * t4]);
+        af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 2 * t4]);
+        af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][ks + 8 + 2 * t4]);
+        af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][ks + 8 + 2 * t4]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = wn + 8 * j + g;
+        bfr[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 2 * t4]);
+        bfr[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][ks + 8 + 2 * t4]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mma_bf16_16816(acc[i][j], af[i], bfr[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const int m = m0 + wm + 16 * i + g + (h >> 1) * 8, n = n0 + wn + 8 * j + 2 * t4 + (h & 1);
+        if (m >= M || n >= N) continue;
+        if (part) {
+          part[((int64_t)blockIdx.z * M + m) * N + n] = acc[i][j][h];
+        } else {
+          float v = alpha * acc[i][j][h];
+          if (beta != 0.0f) v += beta * C[(int64_t)m * ldc + n];
+          C[(int64_t)m * ldc + n] = v;
+        }
+      }
+}
+
+__global__ void hgemm_reduce_kernel(const float* __restrict__ part, int splits, int M, int N, float alpha,
+                                    float beta, float* __restrict__ C, int64_t ldc) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)M * N; t += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.0f;
+    for (int z = 0; z < splits; ++z) s += part[(int64_t)z * M * N + t];
+    const int64_t m = t / N, n = t - m * N;
+    float v = alpha * s;
+    if (beta != 0.0f) v += beta * C[m * ldc + n];
+    C[m * ldc + n] = v;
+  }
+}
+
+// Tensor-core GEMM with the sgemm argument convention; splits K when the
+// output has fewer tiles than the GPU has SMs (partials in `work`, grown as
+// needed).
+template <class TA, class TB>
+void hgemm(int M, int N, int K, float alpha, const TA* A, int64_t sam, int64_t sak, const TB* B, int64_t sbk,
+           int64_t sbn, float beta, float* C, int64_t ldc, DBuf<float>& work, cudaStream_t s) {
+  const int tiles = ((N + HT - 1) / HT) * ((M + HT - 1) / HT);
+  int splits = 1;
+  if (tiles < 152 && K >= 8 * HK) splits = std::min((2 * 152 + tiles - 1) / tiles, K / (4 * HK));
+  splits = std::max(1, std::min(splits, 256));
+  const int kchunk = ((K + splits - 1) / splits + HK - 1) / HK * HK;
+  splits = (K + kchunk - 1) / kchunk;
+  dim3 grid((N + HT - 1) / HT, (M + HT - 1) / HT, splits);
+  if (splits == 1) {
+    hgemm_kernel<TA, TB><<<grid, 128, 0, s>>>(M, N, K, kchunk, alpha, A, sam, sak, B, sbk, sbn, beta, C, ldc, nullptr);
+    FCC_CHECK_LAUNCH();
+    return;
+  }
+  const int64_t need = (int64_t)splits * M * N;
+  if ((int64_t)work.n < need) work.alloc(need);
+  hgemm_kernel<TA, TB><<<grid, 128, 0, s>>>(M, N, K, kchunk, alpha, A, sam, sak, B, sbk, sbn, beta, C, ldc, work.p);
+  FCC_CHECK_LAUNCH();
+  hgemm_reduce_kernel<<<(unsigned)std::min<int64_t>(((int64_t)M * N + 255) / 256, 152 * 4), 256, 0, s>>>(
+      work.p, splits, M, N, alpha, beta, C, ldc);
   FCC_CHECK_LAUNCH();
 }
 
@@ -222,6 +353,73 @@ __global__ void collect_kernel(FeatSrc f, const double* t2, int64_t total, int64
   }
 }
 
+// Thresholded collection in two passes with a fixed sample order: candidate
+// samples are the elements phase + s * stride; a candidate is kept when
+// |t_MP2| >= thresh.  Pass 1 counts the kept candidates of each block's
+// contiguous chunk; pass 2 (after an exclusive scan of the counts on the
+// host) writes them at base + offset[block] + their rank inside the chunk.
+constexpr int CT = 256;
+__device__ __forceinline__ bool keep_elem(const FeatSrc& f, int64_t e, double thresh) {
+  const int v = f.v, o = f.o;
+  const int b = (int)(e % v);
+  int64_t r = e / v;
+  const int a = (int)(r % v);
+  r /= v;
+  const int j = (int)(r % o), i = (int)(r / o);
+  const double D = f.eps[i] + f.eps[j] - f.eps[o + a] - f.eps[o + b];
+  return fabs(f.ovov[(((int64_t)i * v + a) * o + j) * v + b] / D) >= thresh;
+}
+
+__global__ void __launch_bounds__(CT) collect_count_kernel(FeatSrc f, int64_t total, int64_t stride, int64_t phase,
+                                                           int64_t chunk, double thresh, int* counts) {
+  const int64_t ns = (total - phase + stride - 1) / stride;
+  const int64_t s0 = (int64_t)blockIdx.x * chunk, s1 = min(ns, s0 + chunk);
+  int c = 0;
+  for (int64_t sidx = s0 + threadIdx.x; sidx < s1; sidx += CT) c += keep_elem(f, phase + sidx * stride, thresh);
+  __shared__ int sm[CT / 32];
+  for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < CT / 32; ++w) t += sm[w];
+    counts[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(CT) collect_write_kernel(FeatSrc f, const double* t2, int64_t total, int64_t stride,
+                                                           int64_t phase, int64_t chunk, double thresh,
+                                                           const int64_t* offsets, float* X, float* Y, int64_t base) {
+  const int64_t ns = (total - phase + stride - 1) / stride;
+  const int64_t s0 = (int64_t)blockIdx.x * chunk, s1 = min(ns, s0 + chunk);
+  __shared__ int wsum[CT / 32];
+  __shared__ int64_t run;
+  if (threadIdx.x == 0) run = base + offsets[blockIdx.x];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int64_t c0 = s0; c0 < s1; c0 += CT) {
+    const int64_t sidx = c0 + threadIdx.x;
+    const int64_t e = phase + sidx * stride;
+    const bool k = sidx < s1 && keep_elem(f, e, thresh);
+    const unsigned bal = __ballot_sync(0xffffffffu, k);
+    if (lane == 0) wsum[w] = __popc(bal);
+    __syncthreads();
+    int before = 0, all = 0;
+    for (int q = 0; q < CT / 32; ++q) { if (q < w) before += wsum[q]; all += wsum[q]; }
+    const int64_t out = run + before + __popc(bal & ((1u << lane) - 1u));
+    if (k) {
+      float x[NF];
+      double tmp2;
+      features(f, e, x, tmp2);
+      for (int q = 0; q < NF; ++q) X[out * NF + q] = x[q];
+      Y[out] = (float)((t2[e] - tmp2) / (fabs(tmp2) + TARGET_FLOOR));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) run += all;
+    __syncthreads();
+  }
+}
+
 // normalise raw features: (x - mu) / sd
 __global__ void normalise_kernel(const float* Xraw, int64_t n, const float* mu, const float* sd, float* Xn) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n * NF; t += (int64_t)gridDim.x * blockDim.x)
@@ -339,6 +537,7 @@ struct fcc_mlp {
   // batch work buffers
   fcc::DBuf<float> Xb, Yb, Z1, H1, Z2, H2, yb, dy, dH, dH1;
   fcc::DBuf<double> lpart;
+  fcc::DBuf<float> work;                  // split-K partials of the tensor-core products
   int64_t bcap = 0;
 };
 
@@ -361,11 +560,11 @@ double fwd_bwd(fcc_mlp* m, int64_t B, const float* target, bool backward) {
   const __nv_bfloat16* W2 = m->pb.p + OFF_W2;
   const float* b1 = m->p.p + OFF_B1;
   const float* b2 = m->p.p + OFF_B2;
-  // layer 1: Z1 = Xb W1^T   (B x H), K = NF
-  sgemm<float, __nv_bfloat16>((int)B, H, NF, 1.0f, m->Xb.p, NF, 1, W1, 1, NF, 0.0f, m->Z1.p, H, s);
+  // layer 1: Z1 = Xb W1^T   (B x H), K = NF; tensor cores, BF16 operands
+  hgemm<float, __nv_bfloat16>((int)B, H, NF, 1.0f, m->Xb.p, NF, 1, W1, 1, NF, 0.0f, m->Z1.p, H, m->work, s);
   bias_gelu_kernel<<<grid_of(B * H), 256, 0, s>>>(m->Z1.p, m->H1.p, b1, B, H);
   FCC_CHECK_LAUNCH();
-  sgemm<float, __nv_bfloat16>((int)B, H, H, 1.0f, m->H1.p, H, 1, W2, 1, H, 0.0f, m->Z2.p, H, s);
+  hgemm<float, __nv_bfloat16>((int)B, H, H, 1.0f, m->H1.p, H, 1, W2, 1, H, 0.0f, m->Z2.p, H, m->work, s);
   bias_gelu_kernel<<<grid_of(B * H), 256, 0, s>>>(m->Z2.p, m->H2.p, b2, B, H);
   FCC_CHECK_LAUNCH();
   // output layer (w3 FP32 master used directly: 128 weights)
@@ -392,15 +591,15 @@ double fwd_bwd(fcc_mlp* m, int64_t B, const float* target, bool backward) {
   gelu_back_kernel<<<grid_of(B * H), 256, 0, s>>>(m->Z2.p, m->dH.p, B * H);
   FCC_CHECK_LAUNCH();
   // dW2 = dZ2^T H1 (H x H, K = B), db2 = colsum(dZ2)
-  sgemm<float, float>(H, H, (int)B, 1.0f, m->dH.p, 1, H, m->H1.p, H, 1, 0.0f, g + OFF_W2, H, s);
+  hgemm<float, float>(H, H, (int)B, 1.0f, m->dH.p, 1, H, m->H1.p, H, 1, 0.0f, g + OFF_W2, H, m->work, s);
   colsum_kernel<<<H, 256, 0, s>>>(m->dH.p, B, H, g + OFF_B2);
   FCC_CHECK_LAUNCH();
   // dH1 = dZ2 W2 (B x H), dZ1 = dH1 * GELU'(Z1)
-  sgemm<float, __nv_bfloat16>((int)B, H, H, 1.0f, m->dH.p, H, 1, W2, H, 1, 0.0f, m->dH1.p, H, s);
+  hgemm<float, __nv_bfloat16>((int)B, H, H, 1.0f, m->dH.p, H, 1, W2, H, 1, 0.0f, m->dH1.p, H, m->work, s);
   gelu_back_kernel<<<grid_of(B * H), 256, 0, s>>>(m->Z1.p, m->dH1.p, B * H);
   FCC_CHECK_LAUNCH();
   // dW1 = dZ1^T X (H x NF), db1 = colsum(dZ1)
-  sgemm<float, float>(H, NF, (int)B, 1.0f, m->dH1.p, 1, H, m->Xb.p, NF, 1, 0.0f, g + OFF_W1, NF, s);
+  hgemm<float, float>(H, NF, (int)B, 1.0f, m->dH1.p, 1, H, m->Xb.p, NF, 1, 0.0f, g + OFF_W1, NF, m->work, s);
   colsum_kernel<<<H, 256, 0, s>>>(m->dH1.p, B, H, g + OFF_B1);
   FCC_CHECK_LAUNCH();
   return loss;
@@ -542,6 +741,59 @@ int fcc_mlp_collect(fcc_mlp* m, fcc_ctx* c, int32_t stride) {
   });
 }
 
+int fcc_mlp_collect_ex(fcc_mlp* m, fcc_ctx* c, int32_t stride, double thresh) {
+  if (!m || !c || stride < 1 || !(thresh >= 0)) return FCC_ERR_BAD_ARG;
+  if (!c->have_ccsd) return FCC_ERR_STATE;
+  if (c->device != m->device) return FCC_ERR_BAD_ARG;
+  return guard([&]() {
+    FCC_CUDA(cudaSetDevice(m->device));
+    FCC_CUDA(cudaStreamSynchronize(m->stream));
+    cudaStream_t s = c->stream;
+    const int64_t total = c->o * c->o * c->v * c->v;
+    const int64_t phase = (int64_t)(m->nsamp % stride);
+    const int64_t ns = (total - phase + stride - 1) / stride;
+    const int64_t nblk = std::max<int64_t>(1, std::min<int64_t>(152 * 8, (ns + CT - 1) / CT));
+    const int64_t chunk = (ns + nblk - 1) / nblk;
+    DBuf<double> pn;
+    FeatSrc f = feat_src(c, pn);
+    DBuf<int> counts;
+    counts.alloc(nblk);
+    collect_count_kernel<<<(unsigned)nblk, CT, 0, s>>>(f, total, stride, phase, chunk, thresh, counts.p);
+    FCC_CHECK_LAUNCH();
+    std::vector<int> hc(nblk);
+    FCC_CUDA(cudaMemcpyAsync(hc.data(), counts.p, sizeof(int) * nblk, cudaMemcpyDeviceToHost, s));
+    FCC_CUDA(cudaStreamSynchronize(s));
+    std::vector<int64_t> off(nblk);
+    int64_t kept = 0;
+    for (int64_t b = 0; b < nblk; ++b) { off[b] = kept; kept += hc[b]; }
+    if (kept == 0) return FCC_OK;
+    if (m->nsamp + kept > m->cap) {
+      int64_t ncap = std::max<int64_t>(m->cap + m->cap / 2, m->nsamp + kept);
+      DBuf<float> X2, Y2;
+      X2.alloc(ncap * NF);
+      Y2.alloc(ncap);
+      if (m->nsamp) {
+        FCC_CUDA(cudaMemcpy(X2.p, m->X.p, sizeof(float) * m->nsamp * NF, cudaMemcpyDeviceToDevice));
+        FCC_CUDA(cudaMemcpy(Y2.p, m->Y.p, sizeof(float) * m->nsamp, cudaMemcpyDeviceToDevice));
+      }
+      m->X = std::move(X2);
+      m->Y = std::move(Y2);
+      m->cap = ncap;
+    }
+    DBuf<int64_t> doff;
+    doff.alloc(nblk);
+    FCC_CUDA(cudaMemcpyAsync(doff.p, off.data(), sizeof(int64_t) * nblk, cudaMemcpyHostToDevice, s));
+    collect_write_kernel<<<(unsigned)nblk, CT, 0, s>>>(f, c->t2.p, total, stride, phase, chunk, thresh, doff.p, m->X.p,
+                                                       m->Y.p, m->nsamp);
+    FCC_CHECK_LAUNCH();
+    FCC_CUDA(cudaStreamSynchronize(s));
+    m->nsamp += kept;
+    return FCC_OK;
+  });
+}
+
+int64_t fcc_mlp_num_samples(const fcc_mlp* m) { return m ? m->nsamp : -1; }
+
 // Adam training on the collected samples; the first call fixes the feature
 // normalisation (mean and standard deviation of the collected features).
 int fcc_mlp_train(fcc_mlp* m, int32_t steps, int32_t batch, double lr, uint64_t seed, double* loss_log) {
@@ -554,12 +806,14 @@ int fcc_mlp_train(fcc_mlp* m, int32_t steps, int32_t batch, double lr, uint64_t 
       // statistics over an evenly spaced subset of at most 2^20 samples
       const int64_t step = std::max<int64_t>(1, m->nsamp >> 20);
       const int64_t ns = (m->nsamp + step - 1) / step;
-      std::vector<float> X(m->nsamp * NF);
-      FCC_CUDA(cudaMemcpy(X.data(), m->X.p, sizeof(float) * X.size(), cudaMemcpyDeviceToHost));
+      // only the rows used are copied: rows 0, step, 2 step, ...
+      std::vector<float> X(ns * NF);
+      FCC_CUDA(cudaMemcpy2D(X.data(), sizeof(float) * NF, m->X.p, sizeof(float) * NF * step, sizeof(float) * NF, ns,
+                            cudaMemcpyDeviceToHost));
       std::vector<float> ms(2 * NF);
       for (int q = 0; q < NF; ++q) {
         double s1 = 0, s2 = 0;
-        for (int64_t r = 0; r < m->nsamp; r += step) { double x = X[r * NF + q]; s1 += x; s2 += x * x; }
+        for (int64_t r = 0; r < ns; ++r) { double x = X[r * NF + q]; s1 += x; s2 += x * x; }
         double mu = s1 / ns, var = s2 / ns - mu * mu;
         ms[q] = (float)mu;
         ms[NF + q] = (float)(var > 1e-20 ? std::sqrt(var) : 1.0);

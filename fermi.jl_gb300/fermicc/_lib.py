@@ -33,7 +33,8 @@ FCC_TEST_FAULT_NAN = 2
 EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv", "fcc_set_guess",
            "fcc_ccsd_run", "fcc_get_amps", "fcc_triples", "fcc_destroy", "fcc_strerror", "fcc_last_error",
            "fcc_gemm_f64_noalloc", "fcc_mlp_num_params", "fcc_mlp_create", "fcc_mlp_destroy", "fcc_mlp_get_params",
-           "fcc_mlp_set_params", "fcc_mlp_collect", "fcc_mlp_train", "fcc_mlp_grad", "fcc_mlp_guess",
+           "fcc_mlp_set_params", "fcc_mlp_collect", "fcc_mlp_collect_ex", "fcc_mlp_num_samples", "fcc_mlp_train",
+           "fcc_mlp_grad", "fcc_mlp_guess",
            "fcc_mlp_guess_ex", "fcc_checkpoint_save", "fcc_checkpoint_load", "fcc_set_checkpoint",
            "fcc_mp2_energy", "fcc_upload_ao_df", "fcc_upload_ao3_df", "fcc_scf_create", "fcc_scf_destroy",
            "fcc_scf_last_error", "fcc_scf_upload_b", "fcc_scf_fit", "fcc_scf_build_fock", "fcc_scf_build_fock_occ")
@@ -109,6 +110,10 @@ def load():
     lib.fcc_mlp_get_params.argtypes = [vp, fp, i64]
     lib.fcc_mlp_set_params.argtypes = [vp, fp, i64]
     lib.fcc_mlp_collect.argtypes = [vp, vp, i32]
+    lib.fcc_mlp_collect_ex.argtypes = [vp, vp, i32, ctypes.c_double]
+    lib.fcc_mlp_collect_ex.restype = ctypes.c_int
+    lib.fcc_mlp_num_samples.argtypes = [vp]
+    lib.fcc_mlp_num_samples.restype = i64
     lib.fcc_mlp_train.argtypes = [vp, i32, i32, ctypes.c_double, ctypes.c_uint64, dp]
     lib.fcc_mlp_grad.argtypes = [vp, fp, fp, i32, fp, dp]
     lib.fcc_mlp_guess.argtypes = [vp, vp]

@@ -54,8 +54,16 @@ class MLPGuess:
         os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
         self.params().tofile(path)
 
-    def collect(self, context, stride: int = 8):
-        self._check(self.lib.fcc_mlp_collect(self.h, context.h, stride), "fcc_mlp_collect")
+    def collect(self, context, stride: int = 8, thresh: float | None = None):
+        """Samples from a converged context: every stride-th element, or with
+        `thresh` every stride-th of the elements with |t_MP2| >= thresh."""
+        if thresh is None:
+            self._check(self.lib.fcc_mlp_collect(self.h, context.h, stride), "fcc_mlp_collect")
+        else:
+            self._check(self.lib.fcc_mlp_collect_ex(self.h, context.h, stride, thresh), "fcc_mlp_collect_ex")
+
+    def num_samples(self) -> int:
+        return int(self.lib.fcc_mlp_num_samples(self.h))
 
     def train(self, steps: int, batch: int = 65536, lr: float = 1e-3, seed: int = 0) -> np.ndarray:
         log = np.zeros(max(steps, 1))

@@ -200,6 +200,11 @@ int fcc_mlp_get_params(const fcc_mlp* m, float* params, int64_t n);
 int fcc_mlp_set_params(fcc_mlp* m, const float* params, int64_t n);
 /* append training samples (every stride-th element) from a converged CCSD on ctx */
 int fcc_mlp_collect(fcc_mlp* m, fcc_ctx* ctx, int32_t stride);
+/* the same restricted to the elements the guess corrects, |t_MP2| >= thresh
+ * (kept in element order, so the sample set and its order are reproducible) */
+int fcc_mlp_collect_ex(fcc_mlp* m, fcc_ctx* ctx, int32_t stride, double thresh);
+/* number of samples collected so far */
+int64_t fcc_mlp_num_samples(const fcc_mlp* m);
 /* Adam steps on the collected samples (batches drawn with `seed`); loss_log
  * (may be NULL) receives one mean-squared error per step */
 int fcc_mlp_train(fcc_mlp* m, int32_t steps, int32_t batch, double lr, uint64_t seed, double* loss_log);

@@ -4,7 +4,12 @@ initialiser's network, for checking the GPU forward and backward kernels.
 Same parameter layout and arithmetic as the device code: features normalised
 with (mu, sd); W1 and W2 are used rounded to BF16 (the device keeps BF16
 working copies of them), w3 and the biases in FP32; GELU(x) = x Phi(x) with
-the exact normal CDF; loss = mean squared error.
+the exact normal CDF; loss = mean squared error.  With ``bf16_ops=True`` the
+other operand of every tensor-core product is rounded to BF16 as well (the
+device stages both operands of its mma.sync products in BF16): the
+normalised features and H1 in the forward pass, dZ2, H1, dZ1 and the
+features in the gradient products.  The output layer (w3) and the bias
+gradients stay unrounded, as on the device.
 """
 from __future__ import annotations
 
@@ -61,20 +66,25 @@ def unpack(p: np.ndarray):
     return W1, b1, W2, b2, w3, b3, mu, sd
 
 
-def forward(p, Xraw):
+def _op(x, bf16_ops):
+    """A tensor-core operand: rounded to BF16 when the device does so."""
+    return bf16_round(np.asarray(x, dtype=np.float32)) if bf16_ops else x
+
+
+def forward(p, Xraw, bf16_ops: bool = False):
     W1, b1, W2, b2, w3, b3, mu, sd = unpack(p)
     X = (np.asarray(Xraw, dtype=np.float64) - mu) / sd
-    Z1 = X @ W1.T + b1
+    Z1 = _op(X, bf16_ops) @ W1.T + b1
     H1 = gelu(Z1)
-    Z2 = H1 @ W2.T + b2
+    Z2 = _op(H1, bf16_ops) @ W2.T + b2
     H2 = gelu(Z2)
     y = H2 @ w3 + b3
     return y, (X, Z1, H1, Z2, H2)
 
 
-def loss_and_grad(p, Xraw, target):
+def loss_and_grad(p, Xraw, target, bf16_ops: bool = False):
     W1, b1, W2, b2, w3, b3, mu, sd = unpack(p)
-    y, (X, Z1, H1, Z2, H2) = forward(p, Xraw)
+    y, (X, Z1, H1, Z2, H2) = forward(p, Xraw, bf16_ops)
     B = len(target)
     d = y - np.asarray(target, dtype=np.float64)
     loss = float(np.mean(d * d))
@@ -83,9 +93,9 @@ def loss_and_grad(p, Xraw, target):
     g[OFF_W3:OFF_B3] = H2.T @ dy
     g[OFF_B3] = dy.sum()
     dZ2 = np.outer(dy, w3) * gelu_grad(Z2)
-    g[OFF_W2:OFF_B2] = (dZ2.T @ H1).ravel()
+    g[OFF_W2:OFF_B2] = (_op(dZ2, bf16_ops).T @ _op(H1, bf16_ops)).ravel()
     g[OFF_B2:OFF_W3] = dZ2.sum(axis=0)
-    dZ1 = (dZ2 @ W2) * gelu_grad(Z1)
-    g[OFF_W1:OFF_B1] = (dZ1.T @ X).ravel()
+    dZ1 = (_op(dZ2, bf16_ops) @ W2) * gelu_grad(Z1)
+    g[OFF_W1:OFF_B1] = (_op(dZ1, bf16_ops).T @ _op(X, bf16_ops)).ravel()
     g[OFF_B1:OFF_W2] = dZ1.sum(axis=0)
     return loss, g

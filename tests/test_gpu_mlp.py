@@ -32,7 +32,9 @@ def test_gradient_matches_cpu_oracle():
     X = rng.standard_normal((257, OM.NF)).astype(np.float32)
     y = rng.standard_normal(257).astype(np.float32)
     loss, g = m.grad(X, y)
-    lref, gref = OM.loss_and_grad(p, X.astype(np.float64), y.astype(np.float64))
+    # the device products are BF16 tensor-core products (mma.sync) with FP32
+    # accumulation: the oracle rounds the same operands to BF16
+    lref, gref = OM.loss_and_grad(p, X.astype(np.float64), y.astype(np.float64), bf16_ops=True)
     assert abs(loss - lref) < 1e-5 * max(1.0, lref)
     g = g[: OM.NTRAIN].astype(np.float64)
     for lo, hi in ((OM.OFF_W1, OM.OFF_B1), (OM.OFF_B1, OM.OFF_W2), (OM.OFF_W2, OM.OFF_B2), (OM.OFF_B2, OM.OFF_W3),
