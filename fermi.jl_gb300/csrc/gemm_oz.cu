@@ -34,7 +34,7 @@ using namespace tc5;
 constexpr int OZ_BM = 128;
 constexpr int OZ_BN = 128;
 constexpr int OZ_BK = 64;
-constexpr int OZ_STAGES = 7;
+constexpr int OZ_STAGES = 6;
 constexpr int OZ_THREADS = 192;      // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int OZ_BITS = 6;           // bits per digit slice
 constexpr int OZ_CH = 32;            // k-blocks per exact FP32 chunk: 2048 products of at most 64*64, |sum| <= 2^23
@@ -42,7 +42,10 @@ constexpr int OZ_MAXPAIRS = 40;
 constexpr int OZ_A_BYTES = OZ_BM * OZ_BK * 2;
 constexpr int OZ_B_BYTES = OZ_BN * OZ_BK * 2;
 constexpr int OZ_STAGE_BYTES = OZ_A_BYTES + OZ_B_BYTES;
-constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE_BYTES + 1024;
+// the final epilogue's 32 x 32 FP64 transpose tile per epilogue warp, beside
+// the operand ring (a persistent CTA is already loading its next unit)
+constexpr int OZ_TILE_BYTES = 4 * 32 * 33 * 8;
+constexpr int OZ_SMEM = OZ_STAGES * OZ_STAGE_BYTES + OZ_TILE_BYTES + 1024;
 constexpr int OZ_COL_LO = 256, OZ_COL_HI = 384;
 
 // Slice pairs in the order of the k loop: by weight group g = sa + sb + 2,
@@ -122,10 +125,35 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32
       : "memory");
 }
 
+// Work unit u of the persistent grid: output tile grouped_tile(u % tiles)
+// and K slice u / tiles (steps [z * steps_per_split, ...) of the step
+// sequence pair-major over k-blocks).
+struct OzUnit {
+  int64_t m0, n0;
+  int st0, st1;
+};
+__device__ __forceinline__ OzUnit oz_unit(int64_t u, int64_t tm, int64_t tn, int total, int steps_per_split) {
+  const int64_t tiles = tm * tn;
+  int64_t mt, nt;
+  grouped_tile(u % tiles, tm, tn, mt, nt);
+  const int z = (int)(u / tiles);
+  OzUnit r;
+  r.m0 = mt * OZ_BM;
+  r.n0 = nt * OZ_BN;
+  r.st0 = z * steps_per_split;
+  r.st1 = min(total, r.st0 + steps_per_split);
+  return r;
+}
+
+// Persistent: CTA b processes units b, b + gridDim.x, ...  The TMA ring and
+// the two chunk accumulators run on across units, so the loads and the MMAs
+// of a unit's first chunks overlap the previous unit's final epilogue (which
+// reads the running sums; only the epilogue warps touch those, in order).
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     gemm_oz_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int nkb,
-                   int kpad, const __grid_constant__ OzPairs pr, int steps_per_split, const int* __restrict__ exA,
-                   const int* __restrict__ exB, int G, EpiMap ep, int* err) {
+                   int kpad, const __grid_constant__ OzPairs pr, int steps_per_split, int64_t tm, int64_t tn,
+                   int64_t units, const int* __restrict__ exA, const int* __restrict__ exB, int G, EpiMap ep,
+                   int* err) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[OZ_STAGES];
   __shared__ __align__(8) uint64_t empty_bar[OZ_STAGES];
@@ -138,7 +166,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* sA = smem;
   uint8_t* sB = smem + OZ_STAGES * OZ_A_BYTES;
+  double* stile = reinterpret_cast<double*>(smem + OZ_STAGES * OZ_STAGE_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int total = pr.n * nkb;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < OZ_STAGES; ++s) {
@@ -163,27 +193,24 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_holder;
-  int64_t mt, nt;
-  grouped_tile(blockIdx.x, (ep.M + OZ_BM - 1) / OZ_BM, (ep.N + OZ_BN - 1) / OZ_BN, mt, nt);
-  const int64_t m0 = mt * OZ_BM;
-  const int64_t n0 = nt * OZ_BN;
-  const int total = pr.n * nkb;
-  const int st0 = (int)blockIdx.z * steps_per_split;
-  const int st1 = min(total, st0 + steps_per_split);
 
   if (warp == 0 && lane == 0) {
     // ---------------- TMA producer
     int it = 0;
-    for (int st = st0; st < st1; ++st, ++it) {
-      const int s = it % OZ_STAGES;
-      const uint32_t ph = (it / OZ_STAGES) & 1;
-      if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1)) { atomicExch(&abort_flag, 1); break; }
-      if (*(volatile int*)&abort_flag) break;
-      const int p = st / nkb, kb = st - p * nkb;
-      const uint32_t fb = smem_u32(&full_bar[s]);
-      mbar_expect_tx(fb, OZ_STAGE_BYTES);
-      tma_load_2d(smem_u32(sA + s * OZ_A_BYTES), &tmA, (int)pr.sa[p] * kpad + kb * OZ_BK, (int32_t)m0, fb);
-      tma_load_2d(smem_u32(sB + s * OZ_B_BYTES), &tmB, (int)pr.sb[p] * kpad + kb * OZ_BK, (int32_t)n0, fb);
+    bool stop = false;
+    for (int64_t u = blockIdx.x; u < units && !stop; u += gridDim.x) {
+      const OzUnit un = oz_unit(u, tm, tn, total, steps_per_split);
+      for (int st = un.st0; st < un.st1; ++st, ++it) {
+        const int s = it % OZ_STAGES;
+        const uint32_t ph = (it / OZ_STAGES) & 1;
+        if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1)) { atomicExch(&abort_flag, 1); stop = true; break; }
+        if (*(volatile int*)&abort_flag) { stop = true; break; }
+        const int p = st / nkb, kb = st - p * nkb;
+        const uint32_t fb = smem_u32(&full_bar[s]);
+        mbar_expect_tx(fb, OZ_STAGE_BYTES);
+        tma_load_2d(smem_u32(sA + s * OZ_A_BYTES), &tmA, (int)pr.sa[p] * kpad + kb * OZ_BK, (int32_t)un.m0, fb);
+        tma_load_2d(smem_u32(sB + s * OZ_B_BYTES), &tmB, (int)pr.sb[p] * kpad + kb * OZ_BK, (int32_t)un.n0, fb);
+      }
     }
     // on an abort, wait (bounded) for the loads still in flight before the
     // shared memory can be released
@@ -196,90 +223,100 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     constexpr uint32_t idesc = idesc_bf16(OZ_BM, OZ_BN);
     int it = 0, chunk = 0;
     bool ok = true;
-    for (int st = st0; st < st1 && ok;) {
-      const int ce = oz_chunk_end(pr, nkb, st, st1);
-      const int b = chunk & 1;
-      if (!mbar_wait(smem_u32(&acce_bar[b]), ((chunk >> 1) & 1) ^ 1)) { atomicExch(&abort_flag, 1); break; }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t dcol = tmem + (uint32_t)(b * OZ_BN);
-      for (int x = st; x < ce; ++x, ++it) {
-        const int s = it % OZ_STAGES;
-        const uint32_t ph = (it / OZ_STAGES) & 1;
-        if (!mbar_wait(smem_u32(&full_bar[s]), ph)) { atomicExch(&abort_flag, 1); ok = false; break; }
+    for (int64_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
+      const OzUnit un = oz_unit(u, tm, tn, total, steps_per_split);
+      for (int st = un.st0; st < un.st1 && ok;) {
+        const int ce = oz_chunk_end(pr, nkb, st, un.st1);
+        const int b = chunk & 1;
+        if (!mbar_wait(smem_u32(&acce_bar[b]), ((chunk >> 1) & 1) ^ 1)) { atomicExch(&abort_flag, 1); ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint64_t ad = sw128_desc(smem_u32(sA + s * OZ_A_BYTES));
-        const uint64_t bd = sw128_desc(smem_u32(sB + s * OZ_B_BYTES));
+        const uint32_t dcol = tmem + (uint32_t)(b * OZ_BN);
+        for (int x = st; x < ce; ++x, ++it) {
+          const int s = it % OZ_STAGES;
+          const uint32_t ph = (it / OZ_STAGES) & 1;
+          if (!mbar_wait(smem_u32(&full_bar[s]), ph)) { atomicExch(&abort_flag, 1); ok = false; break; }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint64_t ad = sw128_desc(smem_u32(sA + s * OZ_A_BYTES));
+          const uint64_t bd = sw128_desc(smem_u32(sB + s * OZ_B_BYTES));
 #pragma unroll
-        for (int kk = 0; kk < OZ_BK / 16; ++kk) {
-          const uint32_t acc = (x > st || kk > 0) ? 1u : 0u;
-          asm volatile(
-              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dcol),
-              "l"(ad + (uint64_t)(2 * kk)), "l"(bd + (uint64_t)(2 * kk)), "r"(idesc), "r"(acc)
-              : "memory");
+          for (int kk = 0; kk < OZ_BK / 16; ++kk) {
+            const uint32_t acc = (x > st || kk > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dcol),
+                "l"(ad + (uint64_t)(2 * kk)), "l"(bd + (uint64_t)(2 * kk)), "r"(idesc), "r"(acc)
+                : "memory");
+          }
+          tc_commit(smem_u32(&empty_bar[s]));
         }
-        tc_commit(smem_u32(&empty_bar[s]));
+        if (!ok) break;
+        tc_commit(smem_u32(&accf_bar[b]));
+        st = ce;
+        ++chunk;
       }
-      if (!ok) break;
-      tc_commit(smem_u32(&accf_bar[b]));
-      st = ce;
-      ++chunk;
     }
     tc_commit(smem_u32(&done_bar));
   } else if (warp >= 2) {
-    // ---------------- epilogue warps: rows q*32 .. q*32+31 of the tile
+    // ---------------- epilogue warps: rows q*32 .. q*32+31 of each tile
     const int q = warp & 3;
     const uint32_t lanebase = tmem + ((uint32_t)(q * 32) << 16);
+    double (*tile)[33] = reinterpret_cast<double (*)[33]>(stile + q * 32 * 33);
     bool ok = true;
-    int chunk = 0;
-    for (int st = st0; st < st1;) {
-      const int ce = oz_chunk_end(pr, nkb, st, st1);
-      const int g = pr.g[st / nkb];
-      const int b = chunk & 1;
-      ok = mbar_wait(smem_u32(&accf_bar[b]), (chunk >> 1) & 1);
-      ok = __all_sync(0xffffffffu, ok);
-      if (!ok || __any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0)) { atomicExch(&abort_flag, 1); ok = false; break; }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // weight of the group, 2^(-6g), exact in FP32
-      const float wg = __int_as_float((127 - OZ_BITS * g) << 23);
+    int chunk = 0;   // over all units: the accumulator and its barrier phase
+    // alpha = +-2^ka folds into the exponent arithmetic; otherwise one FP64 multiply
+    const unsigned long long ab = (unsigned long long)__double_as_longlong(ep.alpha);
+    const bool apow2 = (ab & ((1ull << 52) - 1)) == 0 && ((ab >> 52) & 0x7FF) != 0;
+    const int ka = apow2 ? (int)((ab >> 52) & 0x7FF) - 1023 : 0;
+    const bool aneg = apow2 && (ab >> 63);
+    for (int64_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
+      const OzUnit un = oz_unit(u, tm, tn, total, steps_per_split);
+      int uchunk = 0;  // chunks of this unit: the first one starts the running sums
+      for (int st = un.st0; st < un.st1;) {
+        const int ce = oz_chunk_end(pr, nkb, st, un.st1);
+        const int g = pr.g[st / nkb];
+        const int b = chunk & 1;
+        ok = mbar_wait(smem_u32(&accf_bar[b]), (chunk >> 1) & 1);
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok || __any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0)) { atomicExch(&abort_flag, 1); ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // weight of the group, 2^(-6g), exact in FP32
+        const float wg = __int_as_float((127 - OZ_BITS * g) << 23);
 #pragma unroll 1
-      for (int c0 = 0; c0 < OZ_BN; c0 += 32) {
-        uint32_t acc[32], hi[32], lo[32];
-        tmem_ld32(lanebase + (uint32_t)(b * OZ_BN + c0), acc);
-        if (chunk > 0) {
-          tmem_ld32(lanebase + (uint32_t)(OZ_COL_HI + c0), hi);
-          tmem_ld32(lanebase + (uint32_t)(OZ_COL_LO + c0), lo);
-        }
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        for (int c0 = 0; c0 < OZ_BN; c0 += 32) {
+          uint32_t acc[32], hi[32], lo[32];
+          tmem_ld32(lanebase + (uint32_t)(b * OZ_BN + c0), acc);
+          if (uchunk > 0) {
+            tmem_ld32(lanebase + (uint32_t)(OZ_COL_HI + c0), hi);
+            tmem_ld32(lanebase + (uint32_t)(OZ_COL_LO + c0), lo);
+          }
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int jj = 0; jj < 32; ++jj) {
-          // the chunk sum is an exact integer below 2^22; times 2^(-6g) exact
-          const float v = __fmul_rn(__uint_as_float(acc[jj]), wg);
-          float h = chunk > 0 ? __uint_as_float(hi[jj]) : 0.0f;
-          float l = chunk > 0 ? __uint_as_float(lo[jj]) : 0.0f;
-          ff_add(h, l, v);
-          hi[jj] = __float_as_uint(h);
-          lo[jj] = __float_as_uint(l);
+          for (int jj = 0; jj < 32; ++jj) {
+            // the chunk sum is an exact integer below 2^22; times 2^(-6g) exact
+            const float v = __fmul_rn(__uint_as_float(acc[jj]), wg);
+            float h = uchunk > 0 ? __uint_as_float(hi[jj]) : 0.0f;
+            float l = uchunk > 0 ? __uint_as_float(lo[jj]) : 0.0f;
+            ff_add(h, l, v);
+            hi[jj] = __float_as_uint(h);
+            lo[jj] = __float_as_uint(l);
+          }
+          tmem_st32(lanebase + (uint32_t)(OZ_COL_HI + c0), hi);
+          tmem_st32(lanebase + (uint32_t)(OZ_COL_LO + c0), lo);
         }
-        tmem_st32(lanebase + (uint32_t)(OZ_COL_HI + c0), hi);
-        tmem_st32(lanebase + (uint32_t)(OZ_COL_LO + c0), lo);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&acce_bar[b]));
+        st = ce;
+        ++chunk;
+        ++uchunk;
       }
-      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(smem_u32(&acce_bar[b]));
-      st = ce;
-      ++chunk;
-    }
-    // every MMA is complete before TMEM is read for the last time or freed
-    bool dn = mbar_wait(smem_u32(&done_bar), 0);
-    dn = __all_sync(0xffffffffu, dn);
-    if (!dn) atomicExch(&abort_flag, 1);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const bool abort_now = __any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0);
-    if (ok && dn && !abort_now && chunk > 0) {
+      if (!ok || uchunk == 0) break;
+      // ---- final epilogue of the unit: the running sums, scaled, to C (the
+      // unit's last chunk barrier covered every MMA of the unit; the sums were
+      // written by this warp, whose stores have completed)
       const int row = q * 32 + lane;
-      const int64_t m = m0 + row;
+      const int64_t m = un.m0 + row;
       int64_t crow = 0;
       int erow = 0;
       if (m < ep.M) {
@@ -288,23 +325,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         crow = m1 * ep.ms1 + m2 * ep.ms2 + m3 * ep.ms3;
         erow = oz_row_exp(exA[m]);
       }
-      // alpha = +-2^ka folds into the exponent arithmetic; otherwise one FP64 multiply
-      const unsigned long long ab = (unsigned long long)__double_as_longlong(ep.alpha);
-      const bool apow2 = (ab & ((1ull << 52) - 1)) == 0 && ((ab >> 52) & 0x7FF) != 0;
-      const int ka = apow2 ? (int)((ab >> 52) & 0x7FF) - 1023 : 0;
-      const bool aneg = apow2 && (ab >> 63);
-      // per epilogue warp a 32 x 32 FP64 transpose tile, in the operand ring
-      // (every load has been consumed once done_bar has completed)
-      double (*tile)[33] = reinterpret_cast<double (*)[32][33]>(smem)[q];
 #pragma unroll 1
       for (int c0 = 0; c0 < OZ_BN; c0 += 32) {
-        if (n0 + c0 >= ep.N) break;
+        if (un.n0 + c0 >= ep.N) break;
         uint32_t hi[32], lo[32];
         tmem_ld32(lanebase + (uint32_t)(OZ_COL_HI + c0), hi);
         tmem_ld32(lanebase + (uint32_t)(OZ_COL_LO + c0), lo);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         // this lane's column exponent, broadcast per column below
-        const int64_t nl = n0 + c0 + lane;
+        const int64_t nl = un.n0 + c0 + lane;
         const int ecl = nl < ep.N ? oz_row_exp(exB[nl]) : 0;
         __syncwarp();
 #pragma unroll
@@ -314,7 +343,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                            f32_to_f64_scaled(__uint_as_float(lo[jj]), e, aneg);
         }
         __syncwarp();
-        const int64_t n = n0 + c0 + lane;
+        const int64_t n = un.n0 + c0 + lane;
         const bool nok = n < ep.N;
         int64_t coff = 0;
         if (nok) {
@@ -325,7 +354,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 #pragma unroll
         for (int jr = 0; jr < 32; ++jr) {
           const int64_t roff = __shfl_sync(0xffffffffu, crow, jr);
-          const int64_t mm = m0 + q * 32 + jr;
+          const int64_t mm = un.m0 + q * 32 + jr;
           if (mm >= ep.M || !nok) continue;
           double val = tile[jr][lane];
           if (!apow2) val *= ep.alpha;
@@ -333,8 +362,13 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
           if (ep.atomic) atomicAdd(dst, val);
           else *dst = val;
         }
+        __syncwarp();
       }
     }
+    // every MMA is complete before TMEM is freed
+    bool dn = mbar_wait(smem_u32(&done_bar), 0);
+    dn = __all_sync(0xffffffffu, dn);
+    if (!dn) atomicExch(&abort_flag, 1);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -547,10 +581,11 @@ void gemm_oz(const __nv_bfloat16* A, int64_t a_rows, const int* exA, const __nv_
   EpiMap e2 = ep;
   e2.atomic = (splits > 1 || ep.beta != 0.0) ? 1 : 0;
   if (e2.atomic && ep.beta != 1.0) scale_output(ep, ep.beta, s);
-  if (tm * tn > 2147483647ll) fail(FCC_ERR_BAD_ARG, "exact-slice grid too large");
-  dim3 grid((unsigned)(tm * tn), 1u, (unsigned)splits);
+  const int64_t units = tiles * splits;
+  const int64_t grid = std::min<int64_t>(units, 152);   // one persistent CTA per SM
   const int pidx = prof_begin(s);
-  gemm_oz_kernel<<<grid, OZ_THREADS, OZ_SMEM, s>>>(ta, tb, nkb, (int)Kpad, pr, per, exA, exB, G, e2, err);
+  gemm_oz_kernel<<<(unsigned)grid, OZ_THREADS, OZ_SMEM, s>>>(ta, tb, nkb, (int)Kpad, pr, per, tm, tn, units, exA, exB,
+                                                             G, e2, err);
   FCC_CHECK_LAUNCH();
   prof_end(s, pidx, PROF_OZ, ep.work > 0 ? ep.work : 2.0 * (double)ep.M * (double)ep.N * (double)(Kpad * pr.n));
 }

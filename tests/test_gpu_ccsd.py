@@ -135,9 +135,11 @@ def test_mixed_form_reaches_the_fp64_fixed_point(n, finish):
     assert precs[0] == 1 and precs[-1] == last       # started split-BF16, ended on the finish
     assert precs == sorted(precs, key=lambda p: (1, 2, last).index(p))   # phases 1 -> 2 -> finish
     assert 2 in precs
-    # the exact-slice residual is accurate enough that the finish passes at
-    # once (allow one more step for an unlucky dE)
-    assert precs.count(last) <= 2, precs
+    # the exact-slice residual is accurate enough that the finish meets the
+    # criteria within a step or two of entering it: the FP64 finish (~25
+    # exact-slice steps each) is entered only once the criteria hold ten
+    # times over, the exact-slice finish as soon as they hold
+    assert precs.count(last) <= (2 if finish == "fp64" else 4), precs
     assert abs(mix.correlation - e64.correlation) < 1e-7
     assert np.abs(mix.T2 - e64.T2).max() < 1e-6
 

@@ -37,9 +37,16 @@ def test_gradient_matches_cpu_oracle():
     lref, gref = OM.loss_and_grad(p, X.astype(np.float64), y.astype(np.float64), bf16_ops=True)
     assert abs(loss - lref) < 1e-5 * max(1.0, lref)
     g = g[: OM.NTRAIN].astype(np.float64)
+    # The device forms the activations in FP32 and the oracle in FP64, so an
+    # operand that lies on a BF16 rounding boundary can round to neighbouring
+    # BF16 values on the two sides: that moves single gradient entries by one
+    # product term times 2^-8.  The bulk agrees to FP32 accumulation order.
     for lo, hi in ((OM.OFF_W1, OM.OFF_B1), (OM.OFF_B1, OM.OFF_W2), (OM.OFF_W2, OM.OFF_B2), (OM.OFF_B2, OM.OFF_W3),
                    (OM.OFF_W3, OM.OFF_B3), (OM.OFF_B3, OM.OFF_B3 + 1)):
-        assert np.abs(g[lo:hi] - gref[lo:hi]).max() <= 2e-4 * max(1e-6, np.abs(gref[lo:hi]).max()), (lo, hi)
+        d = np.abs(g[lo:hi] - gref[lo:hi])
+        scale = max(1e-6, np.abs(gref[lo:hi]).max())
+        assert d.max() <= 1e-3 * scale, (lo, hi, d.max() / scale)
+        assert np.quantile(d, 0.99) <= 2e-5 * scale, (lo, hi, np.quantile(d, 0.99) / scale)
 
 
 def test_training_reduces_loss_and_keeps_the_fixed_point():
