@@ -22,9 +22,19 @@ struct T3Params {
   T3Seg seg[3][T3_NSEG];
   int i, j, k0, nk, o, v;
   int bn;      // B tile width: 128, 160, 192 or 256 (t3_bn(v) unless set for a test)
-  float* G;    // G[g][k - k0][v*v][v], FP32
+  float* G;    // G[g][k - k0] FP32 in 8 x 8 x 8 sub-cube blocks (t3_blk)
   int* err;    // set to 1 if a bounded wait gave up
 };
+
+// Layout of one G_g[k] slab over (pair first index x, pair second index y,
+// lone index z): 8 x 8 x 8 sub-cubes, each 512 contiguous floats, blocks
+// ordered (X, Y, Z) with nb = ceil(v / 8) per index; the energy kernel reads
+// whole sub-cubes with 2 KB loads.
+__host__ __device__ constexpr int64_t t3_nb(int64_t v) { return (v + 7) / 8; }
+__host__ __device__ constexpr int64_t t3_slab(int64_t v) { return t3_nb(v) * t3_nb(v) * t3_nb(v) * 512; }
+__device__ __forceinline__ int64_t t3_blk(int x, int y, int z, int64_t nb) {
+  return ((((int64_t)(x >> 3) * nb + (y >> 3)) * nb + (z >> 3)) << 9) + ((x & 7) << 6) + ((y & 7) << 3) + (z & 7);
+}
 
 // the B tile width used for v virtuals (256 with several column tiles above 256)
 int t3_bn(int v);

@@ -188,8 +188,19 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
       if (!ok || __any_sync(0xffffffffu, *(volatile int*)&abort_flag != 0)) { atomicExch(&abort_flag, 1); break; }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const int64_t m0 = (int64_t)tl.mt * T3_BM;
-      float* out = P.G + ((int64_t)tl.g * P.nk + tl.kq) * v2 * v;
+      const int64_t nbk = t3_nb(v);
+      float* out = P.G + ((int64_t)tl.g * P.nk + tl.kq) * t3_slab(v);
       const int64_t nb0 = (int64_t)tl.nt * BN;
+      // this lane's row (pair (x, y)) offset in the blocked layout; rows are
+      // broadcast to the warp below
+      int64_t myroff = 0;
+      {
+        const int64_t mr = m0 + q * 32 + lane;
+        if (mr < v2) {
+          const int x = (int)(mr / v), y = (int)(mr - (int64_t)x * v);
+          myroff = t3_blk(x, y, 0, nbk);
+        }
+      }
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 32) {
         if (nb0 + c0 >= v) break;
@@ -209,12 +220,12 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
         for (int jj = 0; jj < 32; ++jj) tile[lane][jj] = __uint_as_float(r[jj]);
         __syncwarp();
         const int64_t n = nb0 + c0 + lane;
-        if (n < v) {
+        const int64_t coff = ((n >> 3) << 9) + (n & 7);   // lone index z = n within the (X, Y) block row
 #pragma unroll 4
-          for (int jr = 0; jr < 32; ++jr) {
-            const int64_t m = m0 + q * 32 + jr;
-            if (m < v2) out[m * v + n] = tile[jr][lane];
-          }
+        for (int jr = 0; jr < 32; ++jr) {
+          const int64_t roff = __shfl_sync(0xffffffffu, myroff, jr);
+          const int64_t m = m0 + q * 32 + jr;
+          if (m < v2 && n < v) out[roff + coff] = tile[jr][lane];
         }
       }
       // the accumulator is free for the tile after next

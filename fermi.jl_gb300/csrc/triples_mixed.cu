@@ -5,8 +5,9 @@
 // Same algorithm as the FP64 form (PerturbativeTriples/ijk.jl:20-149),
 // arranged for the tensor cores.  For a pair i >= j and a run of k <= j, the
 // twelve contractions of ijk.jl:109-114 are three grouped products (one per
-// lone virtual index, gemm_t3.cu), written once as G_g[k][pair][lone]:
-//   W_ijk(a,b,c) = G0[k][a][b][c] + G1[k][a][c][b] + G2[k][b][c][a].
+// lone virtual index, gemm_t3.cu), written once as G_g[k] over (pair, lone)
+// in 8 x 8 x 8 sub-cube blocks (t3_blk):
+//   W_ijk(a,b,c) = G0[k](a,b|c) + G1[k](a,c|b) + G2[k](b,c|a).
 // The energy kernel works on 8 x 8 x 8 sub-cubes (a-, b-, c-blocks A >= B >= C):
 // it stages the sub-blocks of G0, G1, G2 for the six permutations of the
 // sub-cube in shared memory with coalesced loads, forms W there, and
@@ -55,10 +56,10 @@ __global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
   const TileTri tt = tiles[blockIdx.x];
   const int oa = tt.a * ET, ob = tt.b * ET, oc = tt.c * ET;
   auto org = [&](int r) { return r == 0 ? oa : (r == 1 ? ob : oc); };
-  const int64_t v2 = (int64_t)v * v, v3 = v2 * v;
-  const float* G0 = G + ((int64_t)0 * nk + kq) * v3;   // [a][b][c]
-  const float* G1 = G + ((int64_t)1 * nk + kq) * v3;   // [a][c][b]
-  const float* G2 = G + ((int64_t)2 * nk + kq) * v3;   // [b][c][a]
+  const int64_t nbk = t3_nb(v), slab = t3_slab(v);
+  const float* G0 = G + ((int64_t)0 * nk + kq) * slab;   // (a, b | c), blocked
+  const float* G1 = G + ((int64_t)1 * nk + kq) * slab;   // (a, c | b)
+  const float* G2 = G + ((int64_t)2 * nk + kq) * slab;   // (b, c | a)
   // permutation p: roles (rx, ry, rz) of the sub-cube blocks, 2 bits each:
   // (0,1,2) (0,2,1) (1,0,2) (1,2,0) (2,0,1) (2,1,0)
   constexpr uint64_t PRC = (0ull | 1ull << 2 | 2ull << 4) | (0ull | 2ull << 2 | 1ull << 4) << 8 |
@@ -81,12 +82,14 @@ __global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
     const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
     const int hi = r / (ET * ET), mid = (r / ET) % ET, lo = r % ET;
     const int o0 = org(role(p, 0)), o1 = org(role(p, 1)), o2 = org(role(p, 2));
-    // G0[x][y][z], z fastest: (x, y, z) = (hi, mid, lo)
-    g0[q] = (o0 + hi < v && o1 + mid < v && o2 + lo < v) ? G0[((int64_t)(o0 + hi) * v + o1 + mid) * v + o2 + lo] : 0.0f;
-    // G1[x][z][y], y fastest: (x, z, y) = (hi, mid, lo)
-    g1[q] = (o0 + hi < v && o1 + lo < v && o2 + mid < v) ? G1[((int64_t)(o0 + hi) * v + o2 + mid) * v + o1 + lo] : 0.0f;
-    // G2[y][z][x], x fastest: (y, z, x) = (hi, mid, lo)
-    g2[q] = (o0 + lo < v && o1 + hi < v && o2 + mid < v) ? G2[((int64_t)(o1 + hi) * v + o2 + mid) * v + o0 + lo] : 0.0f;
+    // the block origins are multiples of 8, so each of the three loads walks
+    // one whole 512-float sub-cube of its G in order (r = hi * 64 + mid * 8 + lo)
+    // G0 (x, y | z): (x, y, z) = (hi, mid, lo)
+    g0[q] = (o0 + hi < v && o1 + mid < v && o2 + lo < v) ? G0[t3_blk(o0 + hi, o1 + mid, o2 + lo, nbk)] : 0.0f;
+    // G1 (x, z | y): (x, z, y) = (hi, mid, lo)
+    g1[q] = (o0 + hi < v && o1 + lo < v && o2 + mid < v) ? G1[t3_blk(o0 + hi, o2 + mid, o1 + lo, nbk)] : 0.0f;
+    // G2 (y, z | x): (y, z, x) = (hi, mid, lo)
+    g2[q] = (o0 + lo < v && o1 + hi < v && o2 + mid < v) ? G2[t3_blk(o1 + hi, o2 + mid, o0 + lo, nbk)] : 0.0f;
   }
 #pragma unroll
   for (int q = 0; q < NM; ++q) {
@@ -311,9 +314,9 @@ double triples_mixed(fcc_ctx* c) {
   // runs of up to KC values of k per launch (G holds 3 * KC * v^3 FP32); long
   // runs keep the launches large (sizing G to stay in L2, 2 k at (H2O)8, was
   // slower overall)
-  const int64_t KC = std::max<int64_t>(1, std::min<int64_t>(16, (1ll << 30) / (3 * v3 * 4)));
+  const int64_t KC = std::max<int64_t>(1, std::min<int64_t>(16, (1ll << 30) / (3 * t3_slab(v) * 4)));
   DBuf<float> G;
-  G.alloc(3 * KC * v3);
+  G.alloc(3 * KC * t3_slab(v));
   P.G = G.p;
   for (int64_t i = 0; i < o; ++i)
     for (int64_t j = 0; j <= i; ++j)

@@ -9,7 +9,7 @@ MP2 amplitude.  The network is trained with Adam (lr 1e-3, batch 65536) by
 the library's own forward, backward and Adam kernels (BF16 tensor-core
 products, FP32 masters) and saved as raw FP32 parameters.
 
-Evaluation: held-out seeds (1000 + k) of (H2O)6 and (H2O)8; from the MP2
+Evaluation: held-out seeds (1000 + k) of (H2O)4, (H2O)6 and (H2O)8; from the MP2
 guess and from the learned guess, in the mixed form and in the plain FP64
 form, to a 1e-8 residual with the energy converged to 1e-10; reports the
 iterations, the converged energies and the guess errors.
@@ -65,7 +65,7 @@ def input_stream(cases, workers):
         pool.join()
 
 
-def solve(inp, guess_model=None, precision="fp64", max_rms=1e-8, e_conv=1e-8):
+def solve(inp, guess_model=None, precision="fp64", max_rms=1e-8, e_conv=1e-8, lam=None, thresh=None):
     from . import Options, RCCSD
     from .rccsd import Context
     Options.reset()
@@ -75,7 +75,7 @@ def solve(inp, guess_model=None, precision="fp64", max_rms=1e-8, e_conv=1e-8):
     Options.set("cc_max_iter", 100)
     ctx = Context(inp)
     if guess_model is not None:
-        guess_model.guess(ctx)
+        guess_model.guess(ctx, lam, thresh)
         T1g, T2g = ctx.amplitudes()
         r = RCCSD.compute(inp, T1g, T2g, context=ctx)
     else:
@@ -103,21 +103,22 @@ def build_training_set(model, cases, strides, workers=8, log=print, every=32):
                             "wall_s": time.time() - t0, "solve_s": gpu_s, "host_inputs_s": host_s}), flush=True)
 
 
-def evaluate(model, cases, precision, workers=8, log=print):
+def evaluate(model, cases, precision, workers=8, log=print, lam=None, thresh=None):
     """Per held-out geometry: iterations from the MP2 and from the learned
-    guess (same criteria), the converged energies and the T2 guess errors."""
+    guess (same criteria), the converged energies and the T2 guess errors
+    (lam, thresh: a scaled correction applied where |t_MP2| >= thresh)."""
     out = []
     for waters, sd, inp, _ in input_stream(cases, workers):
         ref, ctx = solve(inp, precision=precision, e_conv=1e-10)
         T2c = ref.T2
         ctx.lib.fcc_set_guess(ctx.h, None, None)
         _, T2mp2 = ctx.amplitudes()
-        model.guess(ctx)
+        model.guess(ctx, lam, thresh)
         _, T2mlp = ctx.amplitudes()
         err_mp2 = float(np.sqrt(np.mean((T2mp2 - T2c) ** 2)))
         err_mlp = float(np.sqrt(np.mean((T2mlp - T2c) ** 2)))
         ctx.close()
-        lrn, ctx2 = solve(inp, guess_model=model, precision=precision, e_conv=1e-10)
+        lrn, ctx2 = solve(inp, guess_model=model, precision=precision, e_conv=1e-10, lam=lam, thresh=thresh)
         ctx2.close()
         row = dict(precision=precision, waters=waters, seed=sd, iters_mp2=len(ref.iterations),
                    iters_mlp=len(lrn.iterations), time_mp2=sum(l["seconds"] for l in ref.iterations),
@@ -154,6 +155,8 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--out", default="mlp_t2_guess.f32")
+    ap.add_argument("--eval4", type=int, default=0, help="held-out (H2O)4 seeds, mixed form")
+    ap.add_argument("--fp64-eval4", type=int, default=0, help="held-out (H2O)4 seeds, FP64 form")
     ap.add_argument("--eval6", type=int, default=4, help="held-out (H2O)6 seeds, mixed form")
     ap.add_argument("--eval8", type=int, default=2, help="held-out (H2O)8 seeds, mixed form")
     ap.add_argument("--fp64-eval6", type=int, default=0, help="held-out (H2O)6 seeds, FP64 form")
@@ -161,6 +164,8 @@ def main():
     ap.add_argument("--eval-only", action="store_true",
                     help="evaluate the packaged network (fermicc/data) or --params instead of training one")
     ap.add_argument("--params", default=None)
+    ap.add_argument("--lam", type=float, default=None, help="scale of the learned correction (default 1)")
+    ap.add_argument("--thresh", type=float, default=None, help="apply it where |t_MP2| >= this (default 3e-4)")
     a = ap.parse_args()
     from .mlp import DEFAULT_PARAMS, MLPGuess
     if a.eval_only:
@@ -176,11 +181,12 @@ def main():
         model.save(a.out)
         np.savetxt(a.out + ".loss.txt", loss)
     report = {}
-    for prec, n6, n8 in (("mixed", a.eval6, a.eval8), ("fp64", a.fp64_eval6, a.fp64_eval8)):
-        cases = [(6, 1000 + k) for k in range(n6)] + [(8, 1000 + k) for k in range(n8)]
+    for prec, n4, n6, n8 in (("mixed", a.eval4, a.eval6, a.eval8), ("fp64", a.fp64_eval4, a.fp64_eval6, a.fp64_eval8)):
+        cases = ([(4, 1000 + k) for k in range(n4)] + [(6, 1000 + k) for k in range(n6)] +
+                 [(8, 1000 + k) for k in range(n8)])
         if not cases:
             continue
-        rows = evaluate(model, cases, prec, a.workers)
+        rows = evaluate(model, cases, prec, a.workers, lam=a.lam, thresh=a.thresh)
         report[prec] = {"summary": summarise(rows), "rows": rows}
         print(json.dumps({prec: report[prec]["summary"]}), flush=True)
     if report:

@@ -39,14 +39,18 @@ def test_gradient_matches_cpu_oracle():
     g = g[: OM.NTRAIN].astype(np.float64)
     # The device forms the activations in FP32 and the oracle in FP64, so an
     # operand that lies on a BF16 rounding boundary can round to neighbouring
-    # BF16 values on the two sides: that moves single gradient entries by one
-    # product term times 2^-8.  The bulk agrees to FP32 accumulation order.
+    # BF16 values on the two sides (and such a flip in dZ2 moves a whole row
+    # of dZ1): entries can differ by a few product terms times 2^-8.  Bounded
+    # entry-wise, and the device gradient must be far closer to the oracle
+    # that rounds the same operands than to the unrounded FP64 one.
+    _, g64 = OM.loss_and_grad(p, X.astype(np.float64), y.astype(np.float64), bf16_ops=False)
     for lo, hi in ((OM.OFF_W1, OM.OFF_B1), (OM.OFF_B1, OM.OFF_W2), (OM.OFF_W2, OM.OFF_B2), (OM.OFF_B2, OM.OFF_W3),
                    (OM.OFF_W3, OM.OFF_B3), (OM.OFF_B3, OM.OFF_B3 + 1)):
         d = np.abs(g[lo:hi] - gref[lo:hi])
         scale = max(1e-6, np.abs(gref[lo:hi]).max())
         assert d.max() <= 1e-3 * scale, (lo, hi, d.max() / scale)
-        assert np.quantile(d, 0.99) <= 2e-5 * scale, (lo, hi, np.quantile(d, 0.99) / scale)
+    for lo, hi in ((OM.OFF_W1, OM.OFF_B1), (OM.OFF_W2, OM.OFF_B2)):   # the tensor-core products
+        assert np.linalg.norm(g[lo:hi] - gref[lo:hi]) <= 0.1 * np.linalg.norm(g[lo:hi] - g64[lo:hi]), (lo, hi)
 
 
 def test_training_reduces_loss_and_keeps_the_fixed_point():
@@ -84,3 +88,26 @@ def test_committed_network_beats_the_mp2_guess():
     err_mp2 = np.sqrt(np.mean((T2mp2 - T2c) ** 2))
     err_mlp = np.sqrt(np.mean((T2mlp - T2c) ** 2))
     assert err_mlp < 0.8 * err_mp2, (err_mlp, err_mp2)
+
+
+def test_committed_network_saves_fp64_iterations_on_held_out_clusters():
+    # the packaged network, trained on (H2O)4 seeds 0-511 and (H2O)6 seeds
+    # 0-127, against the MP2 guess on held-out (H2O)4 seeds 1000-1007 in the
+    # plain FP64 form (deterministic): fewer iterations to a 1e-8 residual in
+    # total (the configuration-4 evaluation measured 170 -> 161 here and
+    # 21.1 -> 19.8 per cluster over 24 seeds), the same converged energy
+    from fermicc.mlp import DEFAULT_PARAMS, MLPGuess
+    from fermicc.train_guess import solve
+    m = MLPGuess(0, DEFAULT_PARAMS)
+    it_mp2 = it_mlp = 0
+    for sd in range(1000, 1008):
+        inp = inputs(4, seed=sd)
+        ref, c1 = solve(inp, e_conv=1e-10)
+        lrn, c2 = solve(inp, guess_model=m, e_conv=1e-10)
+        c1.close()
+        c2.close()
+        assert ref.converged and lrn.converged
+        assert abs(ref.energy - lrn.energy) < 1e-9, sd
+        it_mp2 += len(ref.iterations)
+        it_mlp += len(lrn.iterations)
+    assert it_mlp <= it_mp2 - 4, (it_mlp, it_mp2)
