@@ -480,6 +480,10 @@ def main():
         ach = work / ms / scale
         kern[name] = {"launches": int(n), "ms": ms, "achieved": ach, "unit": pk[c][1],
                       "frac": ach / pk[c][0], "ms_per_launch": ms / n}
+    if prof[16] > 0:   # (T) energy kernels: launches, ms, (a >= b >= c) evaluated
+        kern["triples energy kernels (sub-cube permutation sums)"] = {
+            "launches": int(prof[16]), "ms": prof[17], "ms_per_launch": prof[17] / prof[16],
+            "abc_per_s": prof[18] / prof[17] * 1e3 if prof[17] else None}
     dom = max(((c, prof[4 * c + 1]) for c in cls), key=lambda x: x[1])[0]
     n, ms, work = prof[4 * dom], prof[4 * dom + 1], prof[4 * dom + 2]
     ach = work / ms / (1e9 if dom != 2 else 1e6) if ms else None
