@@ -63,9 +63,11 @@ PEAKS_FALLBACK = {"hbm_gbs": 6778.3, "bf16_tflops": 1908.9, "bf16_tflops_sustain
 # its largest launch (the o^3 v^3 ring contraction at (H2O)8, M = N = K = 4864:
 # dram__bytes_read + dram__bytes_write = 7.114e9 + 0.186e9 B for 2 * 4864^3 flop)
 DMMA_DRAM_BYTES_PER_FLOP = (7.114e9 + 0.186e9) / (2.0 * 4864.0 ** 3)
-# the same for the exact-slice kernel (executed BF16 flops), from one ncu
-# capture of an exact-slice ring launch at (H2O)6; None until measured
-OZ_DRAM_BYTES_PER_FLOP = None
+# the same for the exact-slice kernel per executed BF16 flop, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of all 541
+# gemm_oz_kernel launches of one (H2O)8 mixed solve: 359.8e9 + 78.6e9 B for
+# 541 launches of 8.989e11 executed flop on average
+OZ_DRAM_BYTES_PER_FLOP = (359.8e9 + 78.6e9) / (541 * 8.989e11)
 
 
 def parse():
@@ -490,13 +492,14 @@ def main():
     traffic = None
     if dom == 0 and n:
         traffic = DMMA_DRAM_BYTES_PER_FLOP * work / n
-    elif dom == 5 and n and OZ_DRAM_BYTES_PER_FLOP:
+    elif dom == 5 and n:
         traffic = OZ_DRAM_BYTES_PER_FLOP * work / n
     roof = {"bound": "hbm" if dom == 2 else "tensor", "kernel": cls[dom], "achieved": ach,
             "peak": pk[dom][0], "unit": pk[dom][1], "frac": (ach / pk[dom][0]) if ach else None,
             "traffic": traffic,
-            "traffic_note": ("bytes per average launch: the ncu-measured DRAM bytes per flop of a profiled launch "
-                             "times the average launch's flops" if traffic is not None else None),
+            "traffic_note": ("bytes per average launch: ncu-measured DRAM bytes per executed flop (all launches of "
+                             "one solve for the exact-slice kernel, the largest launch for the DMMA kernel) times "
+                             "the average launch's flops" if traffic is not None else None),
             "launches": int(n), "work_per_launch": (work / n) if n else None,
             "peak_source": ("own measurement (DMMA probe; MEASURED_PEAKS.json has no FP64 figure)" if dom == 0
                             else peaks_src + (" (sustained BF16)" if dom != 2 else " (HBM copy)")),

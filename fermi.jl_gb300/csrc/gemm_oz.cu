@@ -75,8 +75,8 @@ OzPairs make_pairs(int G) {
   return p;
 }
 
-// end of the chunk that starts at step st: at most OZ_CH steps, never across
-// a weight group or the end of this CTA's step range
+// end of the chunk that starts at step st (steps pair-major, nkb k-blocks per
+// pair): at most OZ_CH steps, never across a weight group or the end st1
 __device__ __forceinline__ int oz_chunk_end(const OzPairs& pr, int nkb, int st, int st1) {
   const int gend = (int)pr.next[st / nkb] * nkb;
   return min(min(st + OZ_CH, gend), st1);
@@ -126,13 +126,15 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32
 }
 
 // Work unit u of the persistent grid: output tile grouped_tile(u % tiles)
-// and K slice u / tiles (steps [z * steps_per_split, ...) of the step
-// sequence pair-major over k-blocks).
+// over the K range u / tiles (k-blocks [kb0, kb0 + nku)), all slice pairs;
+// the unit's steps are pair-major, st = p * nku + (kb - kb0).  Units running
+// at the same time share one K range, so the operand panels they stream stay
+// in L2 across the slice pairs that reuse them.
 struct OzUnit {
   int64_t m0, n0;
-  int st0, st1;
+  int kb0, nku;
 };
-__device__ __forceinline__ OzUnit oz_unit(int64_t u, int64_t tm, int64_t tn, int total, int steps_per_split) {
+__device__ __forceinline__ OzUnit oz_unit(int64_t u, int64_t tm, int64_t tn, int nkb, int kper) {
   const int64_t tiles = tm * tn;
   int64_t mt, nt;
   grouped_tile(u % tiles, tm, tn, mt, nt);
@@ -140,8 +142,8 @@ __device__ __forceinline__ OzUnit oz_unit(int64_t u, int64_t tm, int64_t tn, int
   OzUnit r;
   r.m0 = mt * OZ_BM;
   r.n0 = nt * OZ_BN;
-  r.st0 = z * steps_per_split;
-  r.st1 = min(total, r.st0 + steps_per_split);
+  r.kb0 = z * kper;
+  r.nku = min(nkb, r.kb0 + kper) - r.kb0;
   return r;
 }
 
@@ -151,7 +153,7 @@ __device__ __forceinline__ OzUnit oz_unit(int64_t u, int64_t tm, int64_t tn, int
 // reads the running sums; only the epilogue warps touch those, in order).
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     gemm_oz_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int nkb,
-                   int kpad, const __grid_constant__ OzPairs pr, int steps_per_split, int64_t tm, int64_t tn,
+                   int kpad, const __grid_constant__ OzPairs pr, int kper, int64_t tm, int64_t tn,
                    int64_t units, const int* __restrict__ exA, const int* __restrict__ exB, int G, EpiMap ep,
                    int* err) {
   extern __shared__ uint8_t smem_raw[];
@@ -168,7 +170,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   uint8_t* sB = smem + OZ_STAGES * OZ_A_BYTES;
   double* stile = reinterpret_cast<double*>(smem + OZ_STAGES * OZ_STAGE_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int total = pr.n * nkb;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < OZ_STAGES; ++s) {
@@ -199,13 +200,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     int it = 0;
     bool stop = false;
     for (int64_t u = blockIdx.x; u < units && !stop; u += gridDim.x) {
-      const OzUnit un = oz_unit(u, tm, tn, total, steps_per_split);
-      for (int st = un.st0; st < un.st1; ++st, ++it) {
+      const OzUnit un = oz_unit(u, tm, tn, nkb, kper);
+      const int nst = pr.n * un.nku;
+      for (int st = 0; st < nst; ++st, ++it) {
         const int s = it % OZ_STAGES;
         const uint32_t ph = (it / OZ_STAGES) & 1;
         if (!mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1)) { atomicExch(&abort_flag, 1); stop = true; break; }
         if (*(volatile int*)&abort_flag) { stop = true; break; }
-        const int p = st / nkb, kb = st - p * nkb;
+        const int p = st / un.nku, kb = un.kb0 + (st - p * un.nku);
         const uint32_t fb = smem_u32(&full_bar[s]);
         mbar_expect_tx(fb, OZ_STAGE_BYTES);
         tma_load_2d(smem_u32(sA + s * OZ_A_BYTES), &tmA, (int)pr.sa[p] * kpad + kb * OZ_BK, (int32_t)un.m0, fb);
@@ -224,9 +226,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     int it = 0, chunk = 0;
     bool ok = true;
     for (int64_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
-      const OzUnit un = oz_unit(u, tm, tn, total, steps_per_split);
-      for (int st = un.st0; st < un.st1 && ok;) {
-        const int ce = oz_chunk_end(pr, nkb, st, un.st1);
+      const OzUnit un = oz_unit(u, tm, tn, nkb, kper);
+      const int nst = pr.n * un.nku;
+      for (int st = 0; st < nst && ok;) {
+        const int ce = oz_chunk_end(pr, un.nku, st, nst);
         const int b = chunk & 1;
         if (!mbar_wait(smem_u32(&acce_bar[b]), ((chunk >> 1) & 1) ^ 1)) { atomicExch(&abort_flag, 1); ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -269,11 +272,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const int ka = apow2 ? (int)((ab >> 52) & 0x7FF) - 1023 : 0;
     const bool aneg = apow2 && (ab >> 63);
     for (int64_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
-      const OzUnit un = oz_unit(u, tm, tn, total, steps_per_split);
+      const OzUnit un = oz_unit(u, tm, tn, nkb, kper);
+      const int nst = pr.n * un.nku;
       int uchunk = 0;  // chunks of this unit: the first one starts the running sums
-      for (int st = un.st0; st < un.st1;) {
-        const int ce = oz_chunk_end(pr, nkb, st, un.st1);
-        const int g = pr.g[st / nkb];
+      for (int st = 0; st < nst;) {
+        const int ce = oz_chunk_end(pr, un.nku, st, nst);
+        const int g = pr.g[st / un.nku];
         const int b = chunk & 1;
         ok = mbar_wait(smem_u32(&accf_bar[b]), (chunk >> 1) & 1);
         ok = __all_sync(0xffffffffu, ok);
@@ -562,20 +566,33 @@ void gemm_oz(const __nv_bfloat16* A, int64_t a_rows, const int* exA, const __nv_
   CUtensorMap tb = tma_map_bf16(B, b_rows, S * Kpad, OZ_BN);
   const int64_t tm = (ep.M + OZ_BM - 1) / OZ_BM, tn = (ep.N + OZ_BN - 1) / OZ_BN;
   const int64_t tiles = tm * tn;
+  // K ranges per tile.  (1) The units that run at the same time (one per SM,
+  // about 8 tile rows x 19 tile columns in the grouped order) share one K
+  // range; their operand panels (all S slices of a 128-row block over the
+  // range) must fit in L2 together, or every slice is fetched again from HBM
+  // for each slice pair that uses it (a full-K ring launch at (H2O)8 read
+  // 17 GB for 0.76 GB of packed operands).  (2) More ranges also fill the GPU
+  // when the output has few tiles; a unit pays a fixed cost (its final
+  // epilogue and the reduction into C) of about 48 k-block steps.
+  const double panel = (double)OZ_BM * S * (double)Kpad * 2.0;
+  const int64_t conc = std::min<int64_t>(tiles, 152);
+  const int64_t rblk = std::min<int64_t>(tm, 8);
+  const int64_t cblk = std::min<int64_t>(tn, (conc + rblk - 1) / rblk);
+  constexpr double L2_BUDGET = 48.0 * (1 << 20);
+  int zl2 = (int)std::ceil((double)(rblk + cblk) * panel / L2_BUDGET);
   const int total = pr.n * nkb;
-  // split the step sequence over CTAs when that shortens the last wave; a CTA
-  // also pays a fixed cost (prologue, final epilogue, reductions into C) of
-  // about 48 k-block steps, so splits stop paying before the waves even out
-  int splits = 1;
+  int zw = 1;
   double best = 1e300;
   constexpr double CTA_FIXED_STEPS = 48.0;
   for (int sp = 1; sp <= 64 && sp * OZ_CH <= total; ++sp) {
     const double waves = std::ceil((double)(tiles * sp) / 152.0);
     const double t = waves * ((double)total / sp + CTA_FIXED_STEPS);
-    if (t < best * 0.97) { best = t; splits = sp; }
+    if (t < best * 0.97) { best = t; zw = sp; }
   }
-  const int per = (total + splits - 1) / splits;
-  splits = (total + per - 1) / per;
+  int splits = std::max(zl2, zw);
+  splits = std::max(1, std::min({splits, 64, std::max(1, nkb / 4)}));
+  const int kper = (nkb + splits - 1) / splits;
+  splits = (nkb + kper - 1) / kper;
   // no loads of C in the kernel: beta = 0 and one K range store, otherwise C
   // is scaled by beta first (not for beta = 1) and the kernel reduces into it
   EpiMap e2 = ep;
@@ -584,8 +601,8 @@ void gemm_oz(const __nv_bfloat16* A, int64_t a_rows, const int* exA, const __nv_
   const int64_t units = tiles * splits;
   const int64_t grid = std::min<int64_t>(units, 152);   // one persistent CTA per SM
   const int pidx = prof_begin(s);
-  gemm_oz_kernel<<<(unsigned)grid, OZ_THREADS, OZ_SMEM, s>>>(ta, tb, nkb, (int)Kpad, pr, per, tm, tn, units, exA, exB,
-                                                             G, e2, err);
+  gemm_oz_kernel<<<(unsigned)grid, OZ_THREADS, OZ_SMEM, s>>>(ta, tb, nkb, (int)Kpad, pr, kper, tm, tn, units, exA,
+                                                             exB, G, e2, err);
   FCC_CHECK_LAUNCH();
   prof_end(s, pidx, PROF_OZ, ep.work > 0 ? ep.work : 2.0 * (double)ep.M * (double)ep.N * (double)(Kpad * pr.n));
 }
