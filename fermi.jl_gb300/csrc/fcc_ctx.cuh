@@ -54,6 +54,7 @@ struct fcc_ctx {
   std::string ckpt_path;
   int32_t ckpt_every = 0;
   int t3_bn_override = 0;     // test hook: B tile width of the mixed (T) GEMM (0: by v)
+  int t3_kc_override = 0;     // test hook: k values per mixed (T) launch (0: the default run length)
   // test hook, one shot: FCC_TEST_FAULT_NO_LOADS makes the next tensor-core
   // GEMM of a CCSD run issue no TMA loads (its bounded waits run out);
   // FCC_TEST_FAULT_NAN writes a NaN into the next doubles residual

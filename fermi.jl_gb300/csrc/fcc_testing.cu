@@ -37,6 +37,12 @@ extern "C" int fcc_test_set_t3_bn(fcc_ctx* c, int32_t bn) {
   return FCC_OK;
 }
 
+extern "C" int fcc_test_set_t3_kc(fcc_ctx* c, int32_t kc) {
+  if (!c || kc < 0 || kc > 64) return FCC_ERR_BAD_ARG;
+  c->t3_kc_override = kc;
+  return FCC_OK;
+}
+
 extern "C" int fcc_test_inject(fcc_ctx* c, int32_t kind) {
   if (!c || !(kind == 0 || kind == FCC_TEST_FAULT_NO_LOADS || kind == FCC_TEST_FAULT_NAN)) return FCC_ERR_BAD_ARG;
   c->test_fault = kind;

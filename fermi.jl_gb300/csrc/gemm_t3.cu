@@ -44,18 +44,29 @@ struct T3Cfg {
 
 __device__ __forceinline__ int t3_sel(int code, int i, int j, int k) { return code == 0 ? i : (code == 1 ? j : k); }
 
-// tile t -> (m-tile, n-tile, group, k - k0), m-tile fastest
+// tile t -> (m-tile, n-tile, group, k - k0), m-tile fastest.  Group 0 comes
+// first for every k of the run (its A operands belong to i and j only, so
+// they stay in L2 across the k sweep); then groups 1 and 2 alternate per k
+// (they share the A operands of k, and each keeps its i- or j-operands).
+// With the group outermost of all, group 0's A panels were evicted between
+// consecutive k and read again from HBM for every k.
 struct T3Tile {
   int mt, nt, g, kq;
 };
-__device__ __forceinline__ T3Tile t3_tile(int t, int tm, int tn) {
+__device__ __forceinline__ T3Tile t3_tile(int t, int tm, int tn, int nk) {
   T3Tile r;
-  r.mt = t % tm;
-  int q = t / tm;
-  r.nt = q % tn;
-  q /= tn;
-  r.g = q % 3;
-  r.kq = q / 3;
+  const int per = tm * tn;
+  const int q = t / per, rem = t - q * per;
+  r.mt = rem % tm;
+  r.nt = rem / tm;
+  if (q < nk) {
+    r.g = 0;
+    r.kq = q;
+  } else {
+    const int q2 = q - nk;
+    r.kq = q2 >> 1;
+    r.g = 1 + (q2 & 1);
+  }
   return r;
 }
 
@@ -112,7 +123,7 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
     int it = 0;
     bool stop = false;
     for (int t = blockIdx.x; t < ntiles && !stop; t += gridDim.x) {
-      const T3Tile tl = t3_tile(t, tm, tn);
+      const T3Tile tl = t3_tile(t, tm, tn, P.nk);
       const int kk = P.k0 + tl.kq;
       const int64_t m0 = (int64_t)tl.mt * T3_BM;
       for (int s = 0; s < T3_NSEG && !stop; ++s) {
@@ -143,7 +154,7 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
     int it = 0, lt = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++lt) {
-      const int g = t3_tile(t, tm, tn).g;
+      const int g = t3_tile(t, tm, tn, P.nk).g;
       int total = 0;
       for (int s = 0; s < T3_NSEG; ++s) total += P.seg[g][s].nkb;
       const int b = lt & 1;
@@ -181,7 +192,7 @@ __global__ void __launch_bounds__(T3_THREADS, 1) gemm_t3_kernel(const __grid_con
     float (*tile)[33] = epi_tile[q];
     int lt = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
-      const T3Tile tl = t3_tile(t, tm, tn);
+      const T3Tile tl = t3_tile(t, tm, tn, P.nk);
       const int b = lt & 1;
       bool ok = mbar_wait(smem_u32(&accf_bar[b]), (lt >> 1) & 1);
       ok = __all_sync(0xffffffffu, ok);

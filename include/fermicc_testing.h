@@ -44,6 +44,11 @@ void* fcc_stream(const fcc_ctx* ctx);
  * (T) GEMM, e.g. to run several column tiles on a small system. */
 int fcc_test_set_t3_bn(fcc_ctx* ctx, int32_t bn);
 
+/* Number of k values per mixed (T) launch (1..64; 0 = the default run
+ * length), e.g. to compare run lengths or to cover several runs on a small
+ * system. */
+int fcc_test_set_t3_kc(fcc_ctx* ctx, int32_t kc);
+
 /* One-shot failure injection on ctx for the error-path tests; nothing here
  * faults the GPU.  FCC_TEST_FAULT_NO_LOADS: the first split-BF16 tensor-core
  * GEMM of the next mixed-form fcc_ccsd_run issues no TMA loads, so its MMA
