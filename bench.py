@@ -115,7 +115,9 @@ def profile_case(args, inp):
         r = RCCSD.compute(inp, context=ctx)
         pt = RCCSDpT.compute(r, inp)
         print(json.dumps({"case": args.profile_case, "wall_s": time.perf_counter() - t0, "e_total": pt.energy,
-                          "kinds": [l["precision"] for l in r.iterations]}))
+                          "kinds": [l["precision"] for l in r.iterations],
+                          "rms": [l["rms"] for l in r.iterations], "dE": [l["dE"] for l in r.iterations],
+                          "seconds": [l["seconds"] for l in r.iterations]}))
     elif args.profile_case == "triples-fp64":
         Options.set("cc_max_iter", 1)
         r = RCCSD.compute(inp, context=ctx)

@@ -607,6 +607,8 @@ void residual(fcc_ctx* c) {
                                                                     c->pairM_o.p, c->pairP_v.p, c->pairM_v.p, nP, nM,
                                                                     nijP, nijM, c->Tp.p, c->Tm.p);
     FCC_CHECK_LAUNCH();
+    // Tp and Tm are the A operands of every block's ladder product: packed once
+    KeepPackedA keep(tc_engine(), c->Tp.p, c->Tm.p);
     auto startP = [&](int64_t a) { return a * v - a * (a - 1) / 2; };   // first (a, b>=a) row
     auto startM = [&](int64_t a) { return a * v - a * (a + 1) / 2; };   // first (a, b>a) row
     for (int64_t a0 = 0; a0 < v; a0 += c->ladder_block) {
@@ -880,12 +882,11 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
       if (kind == K_EXACT9) c->tc.oz_groups = OZ_G_FINISH;
       // exact-slice width by the size of the step: 6 weight groups (15 slice
       // pairs; noise floor in the Jacobi step ~1e-8 at (H2O)8) while the step
-      // is above 100 max_rms, 7 groups (21 pairs, floor ~1e-10) while it is
-      // above max_rms, then 8 groups (28 pairs) to the end.  The width only
-      // grows, so the phase cannot cycle.
+      // is above 100 max_rms, then 7 groups (21 pairs, floor ~1e-10, two
+      // orders below the criteria) until the finish.  The width only grows,
+      // so the phase cannot cycle.
       if (kind == K_EXACT) {
-        const int want = rms < op.max_rms ? OZ_G_DEFAULT
-                                          : (rms < 100.0 * op.max_rms ? OZ_G_DEFAULT - 1 : OZ_G_DEFAULT - 2);
+        const int want = rms < 100.0 * op.max_rms ? OZ_G_DEFAULT - 1 : OZ_G_DEFAULT - 2;
         const int groups = std::max(exact_groups, want);
         if (groups != exact_groups) { best_rms = 1e300; stalled = 0; }
         exact_groups = groups;

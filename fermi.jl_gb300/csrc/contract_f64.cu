@@ -403,6 +403,30 @@ int64_t gdim(const std::vector<Ix>& g) {
 // pad a group to exactly 3 levels (slowest first)
 void pad3(std::vector<Ix>& g) { while (g.size() < 3) g.insert(g.begin(), Ix{1, {0, 0, 0}}); }
 
+bool same_spec(const PackSpec& a, const PackSpec& b) {
+  return a.R == b.R && a.K == b.K && a.Kp == b.Kp && a.rd2 == b.rd2 && a.rd3 == b.rd3 && a.rs1 == b.rs1 &&
+         a.rs2 == b.rs2 && a.rs3 == b.rs3 && a.kd2 == b.kd2 && a.kd3 == b.kd3 && a.ks1 == b.ks1 && a.ks2 == b.ks2 &&
+         a.ks3 == b.ks3 && a.P == b.P && a.code == b.code && a.scale == b.scale;
+}
+
+// The kept pack of operand A for (src, ps, S) when src is one of the
+// engine's kept sources (nullptr otherwise); `fresh` is set when it has to be
+// packed now.
+TcEngine::KeptPack* kept_a(TcEngine* tc, const double* src, const PackSpec& ps, int S, bool& fresh) {
+  fresh = false;
+  for (int i = 0; i < 2; ++i) {
+    if (!src || tc->keep_src[i] != src) continue;
+    TcEngine::KeptPack& k = tc->kept[i];
+    if (k.valid && k.S == S && same_spec(k.ps, ps)) return &k;
+    k.ps = ps;
+    k.S = S;
+    k.valid = true;
+    fresh = true;
+    return &k;
+  }
+  return nullptr;
+}
+
 // Tensor-core evaluation of C = alpha * A.B + beta * C (no batch index).
 void run_tc(TcEngine* tc, double alpha, const TView& A, const TView& B, double beta, const TView& C,
             std::vector<Ix> gm, std::vector<Ix> gn, std::vector<Ix> gk, cudaStream_t s) {
@@ -427,7 +451,21 @@ void run_tc(TcEngine* tc, double alpha, const TView& A, const TView& B, double b
                 gk[1].dim, gk[2].dim, gk[0].s[0], gk[1].s[0], gk[2].s[0], S, 0};
     PackSpec pb{N, K, W, gn[1].dim, gn[2].dim, gn[0].s[1], gn[1].s[1], gn[2].s[1],
                 gk[1].dim, gk[2].dim, gk[0].s[1], gk[1].s[1], gk[2].s[1], S, 0};
-    pack_oz(A.p, pa, S, tc->bufA.p, tc->exA.p, s);
+    bool fresh;
+    TcEngine::KeptPack* ka = kept_a(tc, A.p, pa, S, fresh);
+    __nv_bfloat16* pA = tc->bufA.p;
+    int* eA = tc->exA.p;
+    if (ka) {
+      if (fresh) {
+        if ((int64_t)ka->buf.n < M * W) ka->buf.alloc(M * W);
+        if ((int64_t)ka->ex.n < M) ka->ex.alloc(M);
+        pack_oz(A.p, pa, S, ka->buf.p, ka->ex.p, s);
+      }
+      pA = ka->buf.p;
+      eA = ka->ex.p;
+    } else {
+      pack_oz(A.p, pa, S, pA, eA, s);
+    }
     pack_oz(B.p, pb, S, tc->bufB.p, tc->exB.p, s);
     EpiMap ep;
     ep.M = M; ep.N = N;
@@ -436,7 +474,7 @@ void run_tc(TcEngine* tc, double alpha, const TView& A, const TView& B, double b
     ep.alpha = alpha; ep.beta = beta; ep.C = C.p; ep.mode = EPI_F64;
     const double npairs = (double)(G - 1) * (double)G / 2.0;
     ep.work = 2.0 * (double)M * (double)N * (double)K * npairs;
-    gemm_oz(tc->bufA.p, M, tc->exA.p, tc->bufB.p, N, tc->exB.p, Kpad, G, ep, tc->err, s);
+    gemm_oz(pA, M, eA, tc->bufB.p, N, tc->exB.p, Kpad, G, ep, tc->err, s);
     tc->tc_calls++;
     tc->tc_flops += ep.work;
     return;
@@ -449,7 +487,18 @@ void run_tc(TcEngine* tc, double alpha, const TView& A, const TView& B, double b
               gk[1].dim, gk[2].dim, gk[0].s[0], gk[1].s[0], gk[2].s[0], sc.P, sc.code_a};
   PackSpec pb{N, K, Kp, gn[1].dim, gn[2].dim, gn[0].s[1], gn[1].s[1], gn[2].s[1],
               gk[1].dim, gk[2].dim, gk[0].s[1], gk[1].s[1], gk[2].s[1], sc.P, sc.code_b};
-  pack_split(A.p, pa, tc->bufA.p, s);
+  bool fresh;
+  TcEngine::KeptPack* ka = kept_a(tc, A.p, pa, 0, fresh);
+  __nv_bfloat16* pA = tc->bufA.p;
+  if (ka) {
+    if (fresh) {
+      if ((int64_t)ka->buf.n < M * Kp) ka->buf.alloc(M * Kp);
+      pack_split(A.p, pa, ka->buf.p, s);
+    }
+    pA = ka->buf.p;
+  } else {
+    pack_split(A.p, pa, pA, s);
+  }
   pack_split(B.p, pb, tc->bufB.p, s);
   EpiMap ep;
   ep.M = M; ep.N = N;
@@ -459,7 +508,7 @@ void run_tc(TcEngine* tc, double alpha, const TView& A, const TView& B, double b
   ep.work = 2.0 * (double)M * (double)N * (double)K * sc.P;
   ep.no_loads = tc->no_loads_once;
   tc->no_loads_once = 0;
-  gemm_bf16x3(tc->bufA.p, M, 0, tc->bufB.p, N, 0, Kp, ep, tc->err, s);
+  gemm_bf16x3(pA, M, 0, tc->bufB.p, N, 0, Kp, ep, tc->err, s);
   tc->tc_calls++;
   tc->tc_flops += 2.0 * (double)M * (double)N * (double)K * sc.P;
 }

@@ -3,6 +3,8 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "fcc_common.cuh"
 
 namespace fcc {
@@ -66,6 +68,51 @@ struct PackColIter {
     off += ps.ks1 - ps.kd2 * ps.ks2;   // from (k1, kd2, 0) to (k1 + 1, 0, 0)
   }
 };
+
+// k is one source index (k3 = k): column offset k * ks3, no divisions
+__host__ __device__ inline bool pack_k_single(const PackSpec& ps) { return ps.kd2 == 1 && ps.kd3 >= ps.K; }
+
+// Source values of packed columns k0 .. k0 + cnt - 1 (cnt <= 4) of the row at
+// source offset ro; zeros past cnt.
+__device__ __forceinline__ void pack_load4(const double* __restrict__ src, const PackSpec& ps, bool k1, int64_t ro,
+                                           int64_t k0, int cnt, double (&x)[4]) {
+  if (k1) {
+    const double* sp = src + ro + k0 * ps.ks3;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) x[q] = q < cnt ? sp[q * ps.ks3] : 0.0;
+  } else {
+    PackColIter ci(ps, k0);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      x[q] = q < cnt ? src[ro + ci.off] : 0.0;
+      if (q + 1 < cnt) ci.next(ps);
+    }
+  }
+}
+
+// Row walk of the row-major pack kernels: a unit is a segment of gseg
+// 4-column groups of one packed row (nseg segments per row), walked by 2^lg
+// threads (32 ... 256); 256 >> lg units per block of 256 threads.  Rows are
+// cut into segments when there are too few of them to fill the GPU.
+struct PackWalk {
+  int lg;
+  int64_t gseg, nseg;
+};
+inline PackWalk pack_walk(int64_t R, int64_t groups) {
+  PackWalk w;
+  w.lg = 5;
+  while (w.lg < 8 && (int64_t(1) << w.lg) < groups) ++w.lg;
+  const int64_t tpr = int64_t(1) << w.lg;
+  // about 152 SMs x 2048 threads, up to 8 groups each
+  const int64_t per_thread = std::max<int64_t>(1, std::min<int64_t>(8, R * groups / (152 * 2048)));
+  w.gseg = std::min(groups, tpr * per_thread);
+  w.nseg = (groups + w.gseg - 1) / w.gseg;
+  return w;
+}
+inline unsigned pack_walk_grid(const PackWalk& w, int64_t R) {
+  const int64_t upb = 256 >> w.lg;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((R * w.nseg + upb - 1) / upb, 152 * 32));
+}
 
 // Output scatter of the GEMM: element (m, n) goes to
 // C[m1*ms1 + m2*ms2 + m3*ms3 + n1*ns1 + n2*ns2 + n3*ns3] as
@@ -136,8 +183,39 @@ struct TcEngine {
   DBuf<__nv_bfloat16> bufA, bufB;
   int* err = nullptr;
   int no_loads_once = 0;   // test hook: the next split-BF16 GEMM runs with EpiMap::no_loads
+  // Packed A operands kept across calls: an A operand whose source is one of
+  // keep_src (set by a KeepPackedA scope, whose caller guarantees that those
+  // sources do not change meanwhile) is packed into its own entry and packed
+  // again only when its layout or slice count changes, so an operand used by
+  // every block of a loop is packed once.
+  struct KeptPack {
+    PackSpec ps{};
+    int S = 0;
+    bool valid = false;
+    DBuf<__nv_bfloat16> buf;
+    DBuf<int> ex;
+  };
+  const double* keep_src[2] = {nullptr, nullptr};
+  KeptPack kept[2];
   int64_t tc_calls = 0, f64_calls = 0;
   double tc_flops = 0, f64_flops = 0;
+};
+
+// Keep the packed forms of the A operands with sources a0 and a1 over the
+// following contractions; they are dropped when the scope ends.
+struct KeepPackedA {
+  TcEngine* tc;
+  KeepPackedA(TcEngine* e, const double* a0, const double* a1) : tc(e) {
+    if (!tc) return;
+    tc->keep_src[0] = a0;
+    tc->keep_src[1] = a1;
+    for (auto& k : tc->kept) k.valid = false;
+  }
+  ~KeepPackedA() {
+    if (!tc) return;
+    tc->keep_src[0] = tc->keep_src[1] = nullptr;
+    for (auto& k : tc->kept) k.valid = false;
+  }
 };
 
 // Current engine of this host thread (nullptr: every contraction is FP64).

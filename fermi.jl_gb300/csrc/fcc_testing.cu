@@ -162,3 +162,39 @@ extern "C" int fcc_test_split3(const double* x, int64_t R, int64_t K, int32_t ro
     return FCC_ERR_CUDA;
   }
 }
+
+extern "C" int fcc_test_pack_oz(const double* x, int64_t R, int64_t K, int32_t row_fastest, int32_t S, uint16_t* out,
+                                int32_t* ex) {
+  try {
+    if (!x || !out || !ex || R < 1 || K < 1 || S < 1 || S > 8) return FCC_ERR_BAD_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return FCC_ERR_NO_DEVICE;
+    FCC_CUDA(cudaSetDevice(0));
+    cudaStream_t s;
+    FCC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    struct SDel { cudaStream_t s; ~SDel() { cudaStreamDestroy(s); } } sdel{s};
+    fcc::PackSpec ps;
+    ps.R = R;
+    ps.K = K;
+    ps.Kp = fcc::oz_kpad(K);
+    ps.rd2 = 1; ps.rd3 = R; ps.rs1 = 0; ps.rs2 = 0; ps.rs3 = row_fastest ? 1 : K;
+    ps.kd2 = 1; ps.kd3 = K; ps.ks1 = 0; ps.ks2 = 0; ps.ks3 = row_fastest ? R : 1;
+    const int64_t n = R * S * ps.Kp;
+    fcc::DBuf<double> dx;
+    fcc::DBuf<__nv_bfloat16> dy;
+    fcc::DBuf<int> dex;
+    dx.alloc(R * K);
+    dy.alloc(n);
+    dex.alloc(R);
+    FCC_CUDA(cudaMemcpyAsync(dx.p, x, sizeof(double) * R * K, cudaMemcpyHostToDevice, s));
+    fcc::pack_oz(dx.p, ps, S, dy.p, dex.p, s);
+    FCC_CUDA(cudaMemcpyAsync(out, dy.p, sizeof(uint16_t) * n, cudaMemcpyDeviceToHost, s));
+    FCC_CUDA(cudaMemcpyAsync(ex, dex.p, sizeof(int32_t) * R, cudaMemcpyDeviceToHost, s));
+    FCC_CUDA(cudaStreamSynchronize(s));
+    return FCC_OK;
+  } catch (const fcc::Error& e) {
+    return e.code;
+  } catch (...) {
+    return FCC_ERR_CUDA;
+  }
+}

@@ -388,34 +388,52 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 __device__ __forceinline__ int biased_exp(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7FF); }
 
 // ex[r] = max over the row of the biased exponent (ex zeroed before), for
-// sources whose k index is the faster one: a warp per (row, k-slab)
-__global__ void oz_exp_rows_kernel(const double* __restrict__ src, PackSpec ps, int64_t kslab, int* __restrict__ ex) {
+// sources whose k index is the faster one: a warp per (row, k-slab), each
+// lane reading 4 consecutive k at a time
+__global__ void __launch_bounds__(256) oz_exp_rows_kernel(const double* __restrict__ src, PackSpec ps, int64_t kslab,
+                                                          int* __restrict__ ex) {
   const int lane = threadIdx.x & 31;
   const int64_t nks = (ps.K + kslab - 1) / kslab;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const bool k1 = pack_k_single(ps);
   for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < ps.R * nks; w += nw) {
-    const int64_t r = w / nks, k0 = (w % nks) * kslab, k1 = min(ps.K, k0 + kslab);
+    const int64_t r = w / nks, ka = (w % nks) * kslab, kb = min(ps.K, ka + kslab);
     const int64_t ro = pack_row_off(ps, r);
     int m = 0;
-    for (int64_t k = k0 + lane; k < k1; k += 32) m = max(m, biased_exp(src[ro + pack_col_off(ps, k)]));
+    for (int64_t k0 = ka + 4 * lane; k0 < kb; k0 += 128) {
+      double xv[4];
+      pack_load4(src, ps, k1, ro, k0, (int)min((int64_t)4, kb - k0), xv);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) m = max(m, biased_exp(xv[q]));
+    }
     m = __reduce_max_sync(0xffffffffu, m);
     if (lane == 0 && m > 0) atomicMax(ex + r, m);
   }
 }
 
 // same for sources whose row index is the faster one: 32 rows x 8 k-lanes
-// per block over one k-slab
-__global__ void oz_exp_tiles_kernel(const double* __restrict__ src, PackSpec ps, int64_t kslab, int* __restrict__ ex) {
+// per block over one k-slab, the column offsets of each 32-column step in
+// shared memory
+__global__ void __launch_bounds__(256) oz_exp_tiles_kernel(const double* __restrict__ src, PackSpec ps, int64_t kslab,
+                                                           int* __restrict__ ex) {
   __shared__ int red[8][32];
+  __shared__ int64_t coff[32];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int64_t nrt = (ps.R + 31) / 32, nks = (ps.K + kslab - 1) / kslab;
   for (int64_t tb = blockIdx.x; tb < nrt * nks; tb += gridDim.x) {
     const int64_t r = (tb / nks) * 32 + tx;
-    const int64_t k0 = (tb % nks) * kslab, k1 = min(ps.K, k0 + kslab);
+    const int64_t ka = (tb % nks) * kslab, kb = min(ps.K, ka + kslab);
+    const int64_t ro = r < ps.R ? pack_row_off(ps, r) : 0;
     int m = 0;
-    if (r < ps.R) {
-      const int64_t ro = pack_row_off(ps, r);
-      for (int64_t k = k0 + ty; k < k1; k += 8) m = max(m, biased_exp(src[ro + pack_col_off(ps, k)]));
+    for (int64_t kc = ka; kc < kb; kc += 32) {
+      __syncthreads();   // the previous offsets are consumed
+      if (ty == 0) coff[tx] = kc + tx < kb ? pack_col_off(ps, kc + tx) : 0;
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int kk = ty + 8 * j;
+        if (r < ps.R && kc + kk < kb) m = max(m, biased_exp(src[ro + coff[kk]]));
+      }
     }
     red[ty][tx] = m;
     __syncthreads();
@@ -427,11 +445,21 @@ __global__ void oz_exp_tiles_kernel(const double* __restrict__ src, PackSpec ps,
   }
 }
 
-// The S balanced base-64 digits of y = x 2^-e (|x| < 2^e): the integer
-// Z = round(|y| 64^S) is cut into digits d_S..d_2 in [-32, 32) (carrying into
-// the next one) and d_1 = the rest, 0..64; all signed like x.  Integer
-// arithmetic only; |y - sum_s d_s 64^-s| <= 64^-S / 2.
-__device__ __forceinline__ void oz_digits(double x, int e, int S, __nv_bfloat16* d) {
+// bf16 bits of the integer d (|d| < 2^22; exact in bf16 for |d| <= 256): the
+// float 1.5 * 2^23 + d, less the bias, is d exactly, and its top 16 bits are
+// the bf16 of d
+__device__ __forceinline__ uint32_t oz_int_bf16(int d) {
+  return __float_as_uint(__int_as_float(0x4B400000 + d) - 12582912.0f) >> 16;
+}
+
+// The S balanced base-64 digits of y = x 2^-e (|x| < 2^e), as bf16 bits: the
+// integer Z = round(|y| 64^S) is written as d_1 64^(S-1) + ... + d_S with
+// d_S..d_2 in [-32, 32) and d_1 = the rest, 0..64, all signed like x.  The
+// low digits are the plain base-64 digits of Z + 32 (64^(S-2) + ... + 1),
+// less 32 (a digit of Z at or above 32 carries one into the next, as in the
+// sequential cut).  Integer arithmetic only; |y - sum_s d_s 64^-s| <= 64^-S / 2.
+template <int S>
+__device__ __forceinline__ void oz_digits(double x, int e, uint32_t (&d)[S]) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
   const int be = (int)((bits >> 52) & 0x7FF);
   unsigned long long Z = 0;
@@ -441,69 +469,95 @@ __device__ __forceinline__ void oz_digits(double x, int e, int S, __nv_bfloat16*
     if (sh <= 0) Z = m << (-sh);
     else if (sh < 64) Z = (m >> sh) + ((m >> (sh - 1)) & 1ull);
   }
-  const bool neg = (bits >> 63) != 0;
-  for (int s = S - 1; s >= 1; --s) {
-    int r = (int)(Z & 63ull);
-    Z >>= 6;
-    if (r >= 32) { r -= 64; Z += 1; }
-    d[s] = __float2bfloat16_rn((float)(neg ? -r : r));
+  constexpr unsigned long long C = 32ull * (((1ull << (6 * (S - 1))) - 1) / 63);
+  const unsigned long long Zc = Z + C;
+  const int neg = (int)(bits >> 63);
+#pragma unroll
+  for (int s = 1; s < S; ++s) {
+    const int dv = (int)((Zc >> (6 * (S - 1 - s))) & 63ull) - 32;
+    d[s] = oz_int_bf16(neg ? -dv : dv);
   }
-  d[0] = __float2bfloat16_rn((float)(neg ? -(int)Z : (int)Z));
+  const int top = (int)(Zc >> (6 * (S - 1)));
+  d[0] = oz_int_bf16(neg ? -top : top);
 }
 
 constexpr int OZ_MAXS = 8;
 
-// dst[r][s*Kpad + k]: row-major walk, 4 consecutive k of one row per thread
-__global__ void oz_pack_rows_kernel(const double* __restrict__ src, PackSpec ps, int S, int64_t Kpad,
-                                    const int* __restrict__ ex, __nv_bfloat16* __restrict__ dst) {
-  const int64_t kq = Kpad / 4;
-  const int64_t total = ps.R * kq;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = t / kq, k0 = (t - r * kq) * 4;
-    __nv_bfloat16* drow = dst + r * (S * Kpad);
-    __nv_bfloat16 dg[4][OZ_MAXS];
+// dst[r][s*Kpad + k]: row walk (k the faster source index), 2^lg threads per
+// row, each cutting 4 consecutive k and writing one 8-byte word per slice
+// (zeros over the padding [K, Kpad))
+template <int S>
+__global__ void __launch_bounds__(256) oz_pack_rows_kernel(const double* __restrict__ src, PackSpec ps, int64_t Kpad,
+                                                           const int* __restrict__ ex, __nv_bfloat16* __restrict__ dst,
+                                                           PackWalk pw) {
+  const int tpr = 1 << pw.lg, lane = threadIdx.x & (tpr - 1), rpb = 256 >> pw.lg;
+  const int64_t ng = Kpad >> 2;
+  const bool k1 = pack_k_single(ps);
+  const int64_t units = ps.R * pw.nseg;
+  for (int64_t u = (int64_t)blockIdx.x * rpb + (threadIdx.x >> pw.lg); u < units; u += (int64_t)gridDim.x * rpb) {
+    const int64_t r = pw.nseg == 1 ? u : u / pw.nseg;
+    const int64_t g0 = (u - r * pw.nseg) * pw.gseg, g1 = min(ng, g0 + pw.gseg);
     const int e = oz_row_exp(ex[r]);
     const int64_t ro = pack_row_off(ps, r);
-    PackColIter ci(ps, k0 < ps.K ? k0 : 0);
-    for (int qq = 0; qq < 4; ++qq) {
-      const int64_t k = k0 + qq;
-      oz_digits(k < ps.K ? src[ro + ci.off] : 0.0, e, S, dg[qq]);
-      if (k + 1 < ps.K) ci.next(ps);
-    }
-    for (int s = 0; s < S; ++s) {
-      __nv_bfloat162 v0 = __halves2bfloat162(dg[0][s], dg[1][s]);
-      __nv_bfloat162 v1 = __halves2bfloat162(dg[2][s], dg[3][s]);
-      uint2 u;
-      u.x = *reinterpret_cast<uint32_t*>(&v0);
-      u.y = *reinterpret_cast<uint32_t*>(&v1);
-      *reinterpret_cast<uint2*>(drow + s * Kpad + k0) = u;
+    __nv_bfloat16* drow = dst + r * (S * Kpad);
+    for (int64_t g = g0 + lane; g < g1; g += tpr) {
+      const int64_t k0 = g << 2;
+      uint2 w[S];
+      if (k0 < ps.K) {
+        double xv[4];
+        pack_load4(src, ps, k1, ro, k0, (int)min((int64_t)4, ps.K - k0), xv);
+        uint32_t dg[4][S];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) oz_digits<S>(xv[q], e, dg[q]);
+#pragma unroll
+        for (int s = 0; s < S; ++s) w[s] = make_uint2(dg[0][s] | (dg[1][s] << 16), dg[2][s] | (dg[3][s] << 16));
+      } else {
+#pragma unroll
+        for (int s = 0; s < S; ++s) w[s] = make_uint2(0u, 0u);
+      }
+#pragma unroll
+      for (int s = 0; s < S; ++s) *reinterpret_cast<uint2*>(drow + s * Kpad + k0) = w[s];
     }
   }
 }
 
-// transposing walk through a 32 x 32 tile (row index faster in the source)
-__global__ void oz_pack_tiles_kernel(const double* __restrict__ src, PackSpec ps, int S, int64_t Kpad,
-                                     const int* __restrict__ ex, __nv_bfloat16* __restrict__ dst) {
+// transposing walk through 32 x 32 tiles (row index faster in the source):
+// source offsets of the tile's rows and columns in shared memory, coalesced
+// reads along rows, and each thread cuts two consecutive k of one row and
+// writes one 4-byte word per slice (the tiles cover [0, Kpad), zeros past K)
+template <int S>
+__global__ void __launch_bounds__(256) oz_pack_tiles_kernel(const double* __restrict__ src, PackSpec ps, int64_t Kpad,
+                                                            const int* __restrict__ ex,
+                                                            __nv_bfloat16* __restrict__ dst) {
   __shared__ double tile[32][33];
+  __shared__ int64_t roff[32], coff[32];
   const int64_t ntr = (ps.R + 31) / 32, ntk = Kpad / 32;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int kp = threadIdx.x & 15, rw = threadIdx.x >> 4;   // write phase: k pair, row
   for (int64_t tb = blockIdx.x; tb < ntr * ntk; tb += gridDim.x) {
     const int64_t r0 = (tb / ntk) * 32, k0 = (tb % ntk) * 32;
+    __syncthreads();   // the previous tile is consumed
+    if (ty == 0) roff[tx] = r0 + tx < ps.R ? pack_row_off(ps, r0 + tx) : 0;
+    else if (ty == 1) coff[tx] = k0 + tx < ps.K ? pack_col_off(ps, k0 + tx) : 0;
     __syncthreads();
+#pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int kk = ty + 8 * j;
-      const int64_t r = r0 + tx, k = k0 + kk;
-      tile[kk][tx] = (r < ps.R && k < ps.K) ? src[pack_row_off(ps, r) + pack_col_off(ps, k)] : 0.0;
+      tile[kk][tx] = (r0 + tx < ps.R && k0 + kk < ps.K) ? src[roff[tx] + coff[kk]] : 0.0;
     }
     __syncthreads();
-    for (int j = 0; j < 4; ++j) {
-      const int rr = ty + 8 * j;
-      const int64_t r = r0 + rr, k = k0 + tx;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int rr = rw + 16 * j;
+      const int64_t r = r0 + rr;
       if (r >= ps.R) continue;
-      __nv_bfloat16 dg[OZ_MAXS];
-      oz_digits(tile[tx][rr], oz_row_exp(ex[r]), S, dg);
-      __nv_bfloat16* d = dst + r * (S * Kpad) + k;
-      for (int s = 0; s < S; ++s) d[s * Kpad] = dg[s];
+      const int e = oz_row_exp(ex[r]);
+      uint32_t da[S], db[S];
+      oz_digits<S>(tile[2 * kp][rr], e, da);
+      oz_digits<S>(tile[2 * kp + 1][rr], e, db);
+      uint32_t* d = reinterpret_cast<uint32_t*>(dst + r * (S * Kpad) + k0 + 2 * kp);
+#pragma unroll
+      for (int s = 0; s < S; ++s) d[(s * Kpad) >> 1] = da[s] | (db[s] << 16);
     }
   }
 }
@@ -532,21 +586,34 @@ void pack_oz(const double* src, const PackSpec& ps, int S, __nv_bfloat16* dst, i
   int64_t kslab = ps.K;
   if (units < want) kslab = std::max<int64_t>(256, (ps.K * units + want - 1) / want);
   const int64_t nks = (ps.K + kslab - 1) / kslab;
+  const PackWalk pw = pack_walk(ps.R, Kpad / 4);
+  const unsigned rgrid = pack_walk_grid(pw, ps.R);
+  const unsigned tgrid = (unsigned)std::min<int64_t>(((ps.R + 31) / 32) * (Kpad / 32), 152 * 16);
+#define FCC_OZ_PACK(SS)                                                                       \
+  case SS:                                                                                    \
+    if (tiles) oz_pack_tiles_kernel<SS><<<tgrid, 256, 0, s>>>(src, ps, Kpad, ex, dst);         \
+    else oz_pack_rows_kernel<SS><<<rgrid, 256, 0, s>>>(src, ps, Kpad, ex, dst, pw);            \
+    break;
   if (tiles) {
     oz_exp_tiles_kernel<<<(unsigned)std::min<int64_t>(units * nks, 152 * 32), 256, 0, s>>>(src, ps, kslab, ex);
-    FCC_CHECK_LAUNCH();
-    const int64_t nt = ((ps.R + 31) / 32) * (Kpad / 32);
-    oz_pack_tiles_kernel<<<(unsigned)std::min<int64_t>(nt, 152 * 16), 256, 0, s>>>(src, ps, S, Kpad, ex, dst);
-    FCC_CHECK_LAUNCH();
   } else {
     const int64_t warps = units * nks;
     oz_exp_rows_kernel<<<(unsigned)std::min<int64_t>((warps + 7) / 8, 152 * 32), 256, 0, s>>>(src, ps, kslab, ex);
-    FCC_CHECK_LAUNCH();
-    const int64_t tot = ps.R * (Kpad / 4);
-    oz_pack_rows_kernel<<<(unsigned)std::min<int64_t>((tot + 255) / 256, 152 * 32), 256, 0, s>>>(src, ps, S, Kpad, ex,
-                                                                                                 dst);
-    FCC_CHECK_LAUNCH();
   }
+  FCC_CHECK_LAUNCH();
+  switch (S) {
+    FCC_OZ_PACK(1)
+    FCC_OZ_PACK(2)
+    FCC_OZ_PACK(3)
+    FCC_OZ_PACK(4)
+    FCC_OZ_PACK(5)
+    FCC_OZ_PACK(6)
+    FCC_OZ_PACK(7)
+    FCC_OZ_PACK(8)
+    default: fail(FCC_ERR_BAD_ARG, "bad slice count");
+  }
+#undef FCC_OZ_PACK
+  FCC_CHECK_LAUNCH();
 }
 
 void gemm_oz(const __nv_bfloat16* A, int64_t a_rows, const int* exA, const __nv_bfloat16* B, int64_t b_rows,

@@ -69,12 +69,13 @@ __device__ __forceinline__ uint32_t round8(uint64_t a, int& sh) {
 // (typically ~2^-27; pieces below the bf16 range become zero).  Integer arithmetic on the
 // FP64 bit pattern: the remainders are exact and no FP64 instruction (a slow
 // pipe on this part) is issued.
-__device__ __forceinline__ void split3(double x, __nv_bfloat16 (&lv)[3]) {
+__device__ __forceinline__ void split3_int(double x, __nv_bfloat16 (&lv)[3]) {
   const uint64_t u = (uint64_t)__double_as_longlong(x);
   const int ex = (int)((u >> 52) & 0x7FF);
   uint16_t h = 0, m = 0, l = 0;
-  if (ex == 0x7FF) {                         // inf / nan
-    lv[0] = __float2bfloat16_rn((float)x);
+  if (ex == 0x7FF) {                         // inf keeps its sign, nan becomes the canonical bf16 nan
+    const bool nan = (u & ((1ull << 52) - 1)) != 0;
+    lv[0] = __ushort_as_bfloat16(nan ? (unsigned short)0x7FFF : (unsigned short)(((u >> 48) & 0x8000u) | 0x7F80u));
     lv[1] = lv[2] = __ushort_as_bfloat16((unsigned short)0);
     return;
   }
@@ -103,16 +104,74 @@ __device__ __forceinline__ void split3(double x, __nv_bfloat16 (&lv)[3]) {
   lv[2] = __ushort_as_bfloat16(l);
 }
 
+// float of an integer v < 2^23, exactly
+__device__ __forceinline__ float small_uint_float(uint32_t v) { return __uint_as_float(0x4B000000u | v) - 8388608.0f; }
+
+// bf16 bits of the nearest (ties to even) 8-bit value to a * scale, for an
+// integer 0 < a < 2^46 and a power of two scale with a * scale in the normal
+// float range.  a is cut at 24 significant bits with the last one set when
+// anything below is nonzero (rounding to odd, Boldo & Melquiond, IEEE Trans.
+// Comput. 57 (2008)), so that the float-to-bf16 rounding of that float equals
+// the rounding of a itself: a = X + Y with X = (a >> 23) 2^23 and Y < 2^23,
+// both exact floats; s = X + Y rounded toward zero is a cut at 24 bits, and
+// s - X is exact (Sterbenz), so s - X != Y tells whether the cut lost bits.
+__device__ __forceinline__ uint32_t rne8_bits(uint64_t a, float scale) {
+  const float X = small_uint_float((uint32_t)(a >> 23)) * 8388608.0f;
+  const float Y = small_uint_float((uint32_t)a & 0x7FFFFFu);
+  const float sr = __fadd_rz(X, Y);
+  const uint32_t odd = __fsub_rn(sr, X) != Y ? 1u : 0u;
+  const float f = __fmul_rn(__uint_as_float(__float_as_uint(sr) | odd), scale);
+  return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(f));
+}
+
+// integer value of the positive bf16 piece pb in units of 2^e0
+__device__ __forceinline__ uint64_t piece_units(uint32_t pb, int e0) {
+  const uint64_t m8 = 0x80u | (pb & 0x7Fu);
+  const int sh = (int)((pb >> 7) & 0xFFu) - 134 - e0;
+  return sh >= 0 ? m8 << sh : m8 >> (-sh);
+}
+
+// The same three pieces as split3_int, computed with single-precision
+// arithmetic where every piece is a normal float (2^-74 <= |x| < 2^127, so
+// all pieces, multiples of the FP64 ulp of x, are at least 2^-126): the
+// remainders stay exact 64-bit integers in units of that ulp, and each
+// rounding to 8 bits goes through rne8_bits; other x take split3_int.
+__device__ __forceinline__ void split3(double x, __nv_bfloat16 (&lv)[3]) {
+  const uint64_t u = (uint64_t)__double_as_longlong(x);
+  const int ex = (int)((u >> 52) & 0x7FF);
+  if (ex < 949 || ex > 1149) {
+    split3_int(x, lv);
+    return;
+  }
+  const uint32_t sg = (uint32_t)(u >> 63);
+  const int e0 = ex - 1075;                                       // |x| = M 2^e0
+  const uint64_t M = (u & ((1ull << 52) - 1)) | (1ull << 52);
+  // hi: the top 24 bits of M rounded to odd, as a float of the scale of x
+  const uint32_t A = (uint32_t)(M >> 29) | ((M & ((1ull << 29) - 1)) != 0 ? 1u : 0u);
+  const uint32_t hb =
+      (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(__uint_as_float(((uint32_t)(ex - 896) << 23) | (A & 0x7FFFFFu))));
+  const int64_t r1 = (int64_t)M - (int64_t)piece_units(hb, e0);
+  uint32_t m = 0, l = 0;
+  if (r1 != 0) {
+    const float scale = __uint_as_float((uint32_t)(e0 + 127) << 23);   // 2^e0
+    const uint32_t sg1 = sg ^ (r1 < 0 ? 1u : 0u);
+    const uint64_t a1 = (uint64_t)(r1 < 0 ? -r1 : r1);
+    const uint32_t mb = rne8_bits(a1, scale);
+    m = (sg1 << 15) | mb;
+    const int64_t r2 = (int64_t)a1 - (int64_t)piece_units(mb, e0);
+    if (r2 != 0) {
+      const uint32_t sg2 = sg1 ^ (r2 < 0 ? 1u : 0u);
+      l = (sg2 << 15) | rne8_bits((uint64_t)(r2 < 0 ? -r2 : r2), scale);
+    }
+  }
+  lv[0] = __ushort_as_bfloat16((unsigned short)((sg << 15) | hb));
+  lv[1] = __ushort_as_bfloat16((unsigned short)m);
+  lv[2] = __ushort_as_bfloat16((unsigned short)l);
+}
+
 // piece `lev` (0 hi, 1 mid, 2 lo) without a dynamically indexed local array
 __device__ __forceinline__ __nv_bfloat16 piece(const __nv_bfloat16 (&lv)[3], int lev) {
   return lev == 0 ? lv[0] : (lev == 1 ? lv[1] : lv[2]);
-}
-
-// v * scale, with the common scales +-1 as a sign flip on the bit pattern
-__device__ __forceinline__ double scaled(double v, double scale) {
-  if (scale == 1.0) return v;
-  if (scale == -1.0) return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
-  return v * scale;
 }
 
 template <int BN>
@@ -326,76 +385,115 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
 // ---------------------------------------------------------------- packing
 
-// dst[r][k'] (row pitch Kp) from src: piece p of k' = p*K + k holds hi or lo
-// of src(r, k) per `pattern` (bit p set = lo); columns >= 3K are zero.
-// Row-major walk: each thread splits 4 consecutive k of one row once and
-// writes all three pieces (used when k is the faster source index).
-__global__ void pack_rows_kernel(const double* __restrict__ src, PackSpec ps, __nv_bfloat16* __restrict__ dst) {
-  const int64_t kq = (ps.Kp + 3) / 4;   // groups of 4 columns over [0, Kp)
-  const int64_t total = ps.R * kq;
-  const int64_t pk = ps.P * ps.K;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = t / kq, g = t - r * kq;
-    const int64_t k0 = g * 4;
+// Scale modes of the split packing: the source times 1, times -1 (a sign flip
+// of the bit pattern) or times a general factor (one FP64 multiply).
+enum { PK_ONE = 0, PK_NEG = 1, PK_ANY = 2 };
+template <int SM>
+__device__ __forceinline__ double pk_scaled(double v, double scale) {
+  if (SM == PK_ONE) return v;
+  if (SM == PK_NEG) return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
+  return v * scale;
+}
+
+// dst[r][k'] (row pitch Kp) from src: piece p of k' = p*K + k holds hi, mid or
+// lo of src(r, k) per `code`; columns >= P*K are zero.  Row walk (k the
+// faster source index): 2^lg threads per row, each splitting 4 consecutive k
+// once and writing all P pieces, or zeroing 4 of the pad columns.
+template <int SM>
+__global__ void __launch_bounds__(256) pack_rows_kernel(const double* __restrict__ src, PackSpec ps,
+                                                        __nv_bfloat16* __restrict__ dst, PackWalk pw) {
+  const int tpr = 1 << pw.lg, lane = threadIdx.x & (tpr - 1), rpb = 256 >> pw.lg;
+  const int64_t kq = (ps.K + 3) >> 2, pk = ps.P * ps.K;
+  const int64_t ng = kq + ((ps.Kp - pk + 3) >> 2);
+  const bool k1 = pack_k_single(ps);
+  const bool vec = (ps.K & 3) == 0 && (ps.Kp & 3) == 0 && (reinterpret_cast<uintptr_t>(dst) & 7) == 0;
+  const int64_t units = ps.R * pw.nseg;
+  for (int64_t u = (int64_t)blockIdx.x * rpb + (threadIdx.x >> pw.lg); u < units; u += (int64_t)gridDim.x * rpb) {
+    const int64_t r = pw.nseg == 1 ? u : u / pw.nseg;
+    const int64_t g0 = (u - r * pw.nseg) * pw.gseg, g1 = min(ng, g0 + pw.gseg);
+    const int64_t ro = pack_row_off(ps, r);
     __nv_bfloat16* drow = dst + r * ps.Kp;
-    if (k0 < ps.K) {
-      const int64_t ro = pack_row_off(ps, r);
-      __nv_bfloat16 lv[4][3];
-      const int cnt = (int)min((int64_t)4, ps.K - k0);
-      PackColIter ci(ps, k0);
-      for (int q = 0; q < 4; ++q) {
-        split3(q < cnt ? scaled(src[ro + ci.off], ps.scale) : 0.0, lv[q]);
-        if (q + 1 < cnt) ci.next(ps);
-      }
-      for (int p = 0; p < ps.P; ++p) {
-        const int lev = (ps.code >> (2 * p)) & 3;
-        __nv_bfloat16* d = drow + p * ps.K + k0;
-        if (cnt == 4 && (reinterpret_cast<uintptr_t>(d) & 7) == 0) {
-          __nv_bfloat162 v0 = __halves2bfloat162(piece(lv[0], lev), piece(lv[1], lev));
-          __nv_bfloat162 v1 = __halves2bfloat162(piece(lv[2], lev), piece(lv[3], lev));
-          uint2 u;
-          u.x = *reinterpret_cast<uint32_t*>(&v0);
-          u.y = *reinterpret_cast<uint32_t*>(&v1);
-          *reinterpret_cast<uint2*>(d) = u;
-        } else {
+    for (int64_t g = g0 + lane; g < g1; g += tpr) {
+      if (g < kq) {
+        const int64_t k0 = g << 2;
+        const int cnt = (int)min((int64_t)4, ps.K - k0);
+        double xv[4];
+        pack_load4(src, ps, k1, ro, k0, cnt, xv);
+        __nv_bfloat16 lv[4][3];
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
-            if (q < cnt) d[q] = piece(lv[q], lev);
+        for (int q = 0; q < 4; ++q) split3(pk_scaled<SM>(xv[q], ps.scale), lv[q]);
+        for (int p = 0; p < ps.P; ++p) {
+          const int lev = (ps.code >> (2 * p)) & 3;
+          __nv_bfloat16* d = drow + p * ps.K + k0;
+          if (vec && cnt == 4) {
+            __nv_bfloat162 v0 = __halves2bfloat162(piece(lv[0], lev), piece(lv[1], lev));
+            __nv_bfloat162 v1 = __halves2bfloat162(piece(lv[2], lev), piece(lv[3], lev));
+            uint2 u;
+            u.x = *reinterpret_cast<uint32_t*>(&v0);
+            u.y = *reinterpret_cast<uint32_t*>(&v1);
+            *reinterpret_cast<uint2*>(d) = u;
+          } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              if (q < cnt) d[q] = piece(lv[q], lev);
+          }
         }
+      } else {
+        const int64_t c0 = pk + ((g - kq) << 2);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (c0 + q < ps.Kp) drow[c0 + q] = __ushort_as_bfloat16((unsigned short)0);
       }
-    }
-    // zero padding [P*K, Kp)
-    for (int q = 0; q < 4; ++q) {
-      const int64_t kk = pk + k0 + q;
-      if (kk < ps.Kp) drow[kk] = __float2bfloat16_rn(0.0f);
     }
   }
 }
 
-// Transposing walk through a 32 x 32 shared-memory tile, for sources whose
-// row index is the faster one in memory: reads coalesce along rows, writes
-// along k.
-__global__ void pack_tiles_kernel(const double* __restrict__ src, PackSpec ps, __nv_bfloat16* __restrict__ dst) {
+// Transposing walk through 32 x 32 tiles, for sources whose row index is the
+// faster one in memory: the tile's row and column source offsets are
+// computed once into shared memory, reads coalesce along rows, and each
+// thread splits two consecutive k of one row and writes them as one 4-byte
+// store per piece.
+template <int SM>
+__global__ void __launch_bounds__(256) pack_tiles_kernel(const double* __restrict__ src, PackSpec ps,
+                                                         __nv_bfloat16* __restrict__ dst) {
   __shared__ double tile[32][33];
+  __shared__ int64_t roff[32], coff[32];
   const int64_t ntr = (ps.R + 31) / 32, ntk = (ps.K + 31) / 32;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int kp = threadIdx.x & 15, rw = threadIdx.x >> 4;   // write phase: k pair, row
+  const bool pair = (ps.K & 1) == 0 && (ps.Kp & 1) == 0 && (reinterpret_cast<uintptr_t>(dst) & 3) == 0;
   for (int64_t tb = blockIdx.x; tb < ntr * ntk; tb += gridDim.x) {
     const int64_t r0 = (tb / ntk) * 32, k0 = (tb % ntk) * 32;
+    __syncthreads();   // the previous tile is consumed
+    if (ty == 0) roff[tx] = r0 + tx < ps.R ? pack_row_off(ps, r0 + tx) : 0;
+    else if (ty == 1) coff[tx] = k0 + tx < ps.K ? pack_col_off(ps, k0 + tx) : 0;
     __syncthreads();
+#pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int kk = ty + 8 * j;
-      const int64_t r = r0 + tx, k = k0 + kk;
-      tile[kk][tx] = (r < ps.R && k < ps.K) ? scaled(src[pack_row_off(ps, r) + pack_col_off(ps, k)], ps.scale) : 0.0;
+      tile[kk][tx] =
+          (r0 + tx < ps.R && k0 + kk < ps.K) ? pk_scaled<SM>(src[roff[tx] + coff[kk]], ps.scale) : 0.0;
     }
     __syncthreads();
-    for (int j = 0; j < 4; ++j) {
-      const int rr = ty + 8 * j;
-      const int64_t r = r0 + rr, k = k0 + tx;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int rr = rw + 16 * j;
+      const int64_t r = r0 + rr, k = k0 + 2 * kp;
       if (r >= ps.R || k >= ps.K) continue;
-      __nv_bfloat16 lv[3];
-      split3(tile[tx][rr], lv);
+      const bool two = k + 1 < ps.K;
+      __nv_bfloat16 a[3], b[3];
+      split3(tile[2 * kp][rr], a);
+      split3(two ? tile[2 * kp + 1][rr] : 0.0, b);
       __nv_bfloat16* d = dst + r * ps.Kp + k;
-      for (int p = 0; p < ps.P; ++p) d[p * ps.K] = piece(lv, (ps.code >> (2 * p)) & 3);
+      for (int p = 0; p < ps.P; ++p) {
+        const int lev = (ps.code >> (2 * p)) & 3;
+        if (two && pair) {
+          *reinterpret_cast<__nv_bfloat162*>(d + p * ps.K) = __halves2bfloat162(piece(a, lev), piece(b, lev));
+        } else {
+          d[p * ps.K] = piece(a, lev);
+          if (two) d[p * ps.K + 1] = piece(b, lev);
+        }
+      }
     }
   }
 }
@@ -521,9 +619,13 @@ void pack_split(const double* src, const PackSpec& ps, __nv_bfloat16* dst, cudaS
   if (ps.R >= (int64_t(1) << 31) || ps.K >= (int64_t(1) << 31)) fail(FCC_ERR_BAD_ARG, "pack extent too large");
   const int64_t kfast = std::llabs(ps.kd3 > 1 ? ps.ks3 : (ps.kd2 > 1 ? ps.ks2 : ps.ks1));
   const int64_t rfast = std::llabs(ps.rd3 > 1 ? ps.rs3 : (ps.rd2 > 1 ? ps.rs2 : ps.rs1));
+  const int sm = ps.scale == 1.0 ? PK_ONE : (ps.scale == -1.0 ? PK_NEG : PK_ANY);
   if (rfast < kfast && ps.R >= 32) {
     const int64_t tiles = ((ps.R + 31) / 32) * ((ps.K + 31) / 32);
-    pack_tiles_kernel<<<(unsigned)std::min<int64_t>(tiles, 152 * 16), 256, 0, s>>>(src, ps, dst);
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, 152 * 16);
+    if (sm == PK_ONE) pack_tiles_kernel<PK_ONE><<<grid, 256, 0, s>>>(src, ps, dst);
+    else if (sm == PK_NEG) pack_tiles_kernel<PK_NEG><<<grid, 256, 0, s>>>(src, ps, dst);
+    else pack_tiles_kernel<PK_ANY><<<grid, 256, 0, s>>>(src, ps, dst);
     FCC_CHECK_LAUNCH();
     if (ps.Kp > ps.P * ps.K) {
       const int64_t tot = ps.R * (ps.Kp - ps.P * ps.K);
@@ -531,8 +633,11 @@ void pack_split(const double* src, const PackSpec& ps, __nv_bfloat16* dst, cudaS
       FCC_CHECK_LAUNCH();
     }
   } else {
-    const int64_t total = ps.R * ((ps.Kp + 3) / 4);
-    pack_rows_kernel<<<(unsigned)std::min<int64_t>((total + 255) / 256, 152 * 32), 256, 0, s>>>(src, ps, dst);
+    const PackWalk pw = pack_walk(ps.R, (ps.K + 3) / 4 + (ps.Kp - ps.P * ps.K + 3) / 4);
+    const unsigned grid = pack_walk_grid(pw, ps.R);
+    if (sm == PK_ONE) pack_rows_kernel<PK_ONE><<<grid, 256, 0, s>>>(src, ps, dst, pw);
+    else if (sm == PK_NEG) pack_rows_kernel<PK_NEG><<<grid, 256, 0, s>>>(src, ps, dst, pw);
+    else pack_rows_kernel<PK_ANY><<<grid, 256, 0, s>>>(src, ps, dst, pw);
     FCC_CHECK_LAUNCH();
   }
 }

@@ -69,27 +69,41 @@ __global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
   const int t = threadIdx.x;
 
   // ---- stage W = G0[x][y][z] + G1[x][z][y] + G2[y][z][x] and the
-  // integral blocks: every thread first issues all its global loads (each
-  // source read along its stride-1 index), then writes shared memory, so one
-  // global latency covers the whole staging
-  constexpr int NE = 6 * ET * ET * ET / ETH;          // elements per thread per source
+  // integral blocks: every thread first issues all its global loads, then
+  // writes shared memory, so one global latency covers the whole staging.
+  // The block origins are multiples of 8, so each (permutation, group) source
+  // is one whole 512-float sub-cube of its G, read in order as 128 float4
+  // (element r = hi * 64 + mid * 8 + lo of the sub-cube): thread t reads
+  // float4 (t & 127) of the sources q = 0..8, group g = q / 3 and permutation
+  // p = 2 (q - 3g) + (t >> 7).  In the sub-cube, G0 runs over (x, y | z),
+  // G1 over (x, z | y) and G2 over (y, z | x) as (hi, mid, lo).  Elements
+  // past v (v not a multiple of 8: the padding of the blocked layout, inside
+  // the slab but never written) are replaced by zeros.
+  constexpr int NQ = 18 * ET * ET * ET / 4 / ETH;      // float4 per thread (9)
   constexpr int NM = (9 * ET * ET + ETH - 1) / ETH;    // integral elements per thread
-  float g0[NE], g1[NE], g2[NE], mjk[NM], mik[NM], mij[NM];
+  static_assert(NQ == 9 && ETH == 256, "staging assumes 256 threads");
+  float4 gv[NQ];
+  float mjk[NM], mik[NM], mij[NM];
   const int64_t mstr = (int64_t)o * v;
+  const int r0 = (t & 127) << 2;
+  const int shi = r0 >> 6, smid = (r0 >> 3) & 7, slo = r0 & 7;
+  const bool edge = (v & 7) != 0;
 #pragma unroll
-  for (int q = 0; q < NE; ++q) {
-    const int e = t + q * ETH;
-    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
-    const int hi = r / (ET * ET), mid = (r / ET) % ET, lo = r % ET;
+  for (int q = 0; q < NQ; ++q) {
+    const int g = q / 3, p = 2 * (q - 3 * g) + (t >> 7);
     const int o0 = org(role(p, 0)), o1 = org(role(p, 1)), o2 = org(role(p, 2));
-    // the block origins are multiples of 8, so each of the three loads walks
-    // one whole 512-float sub-cube of its G in order (r = hi * 64 + mid * 8 + lo)
-    // G0 (x, y | z): (x, y, z) = (hi, mid, lo)
-    g0[q] = (o0 + hi < v && o1 + mid < v && o2 + lo < v) ? G0[t3_blk(o0 + hi, o1 + mid, o2 + lo, nbk)] : 0.0f;
-    // G1 (x, z | y): (x, z, y) = (hi, mid, lo)
-    g1[q] = (o0 + hi < v && o1 + lo < v && o2 + mid < v) ? G1[t3_blk(o0 + hi, o2 + mid, o1 + lo, nbk)] : 0.0f;
-    // G2 (y, z | x): (y, z, x) = (hi, mid, lo)
-    g2[q] = (o0 + lo < v && o1 + hi < v && o2 + mid < v) ? G2[t3_blk(o1 + hi, o2 + mid, o0 + lo, nbk)] : 0.0f;
+    // sub-cube origin of the source in its own index order (hi, mid, lo)
+    const int b0 = g == 2 ? o1 : o0, b1 = g == 0 ? o1 : o2, b2 = g == 0 ? o2 : (g == 1 ? o1 : o0);
+    const float* src = (g == 0 ? G0 : (g == 1 ? G1 : G2)) + t3_blk(b0, b1, b2, nbk) + r0;
+    float4 x = *reinterpret_cast<const float4*>(src);
+    if (edge) {
+      const bool ok = b0 + shi < v && b1 + smid < v;
+      x.x = ok && b2 + slo < v ? x.x : 0.0f;
+      x.y = ok && b2 + slo + 1 < v ? x.y : 0.0f;
+      x.z = ok && b2 + slo + 2 < v ? x.z : 0.0f;
+      x.w = ok && b2 + slo + 3 < v ? x.w : 0.0f;
+    }
+    gv[q] = x;
   }
 #pragma unroll
   for (int q = 0; q < NM; ++q) {
@@ -123,25 +137,33 @@ __global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
       Mij[rr / 3][rr % 3][qq / ET][qq % ET] = mij[q];
     }
   }
+  // G0 element (hi, mid, lo) is W[p][hi][mid][lo]; G1's is W[p][hi][lo][mid]
+  // (x, z, y order); G2's is W[p][lo][hi][mid] (y, z, x order)
 #pragma unroll
-  for (int q = 0; q < NE; ++q) {
-    const int e = t + q * ETH;
-    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
-    Wt[p][r / (ET * ET)][(r / ET) % ET][r % ET] = g0[q];
+  for (int q = 0; q < 3; ++q) {
+    const int p = 2 * q + (t >> 7);
+    Wt[p][shi][smid][slo] = gv[q].x;
+    Wt[p][shi][smid][slo + 1] = gv[q].y;
+    Wt[p][shi][smid][slo + 2] = gv[q].z;
+    Wt[p][shi][smid][slo + 3] = gv[q].w;
   }
   __syncthreads();
 #pragma unroll
-  for (int q = 0; q < NE; ++q) {
-    const int e = t + q * ETH;
-    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
-    Wt[p][r / (ET * ET)][r % ET][(r / ET) % ET] += g1[q];   // (x, z, y) order
+  for (int q = 3; q < 6; ++q) {
+    const int p = 2 * (q - 3) + (t >> 7);
+    Wt[p][shi][slo][smid] += gv[q].x;
+    Wt[p][shi][slo + 1][smid] += gv[q].y;
+    Wt[p][shi][slo + 2][smid] += gv[q].z;
+    Wt[p][shi][slo + 3][smid] += gv[q].w;
   }
   __syncthreads();
 #pragma unroll
-  for (int q = 0; q < NE; ++q) {
-    const int e = t + q * ETH;
-    const int p = e / (ET * ET * ET), r = e % (ET * ET * ET);
-    Wt[p][r % ET][r / (ET * ET)][(r / ET) % ET] += g2[q];   // (y, z, x) order
+  for (int q = 6; q < 9; ++q) {
+    const int p = 2 * (q - 6) + (t >> 7);
+    Wt[p][slo][shi][smid] += gv[q].x;
+    Wt[p][slo + 1][shi][smid] += gv[q].y;
+    Wt[p][slo + 2][shi][smid] += gv[q].z;
+    Wt[p][slo + 3][shi][smid] += gv[q].w;
   }
   if (t < ET * ET) Dab[t / ET][t % ET] = eps[i] + eps[j] + eps[k] - eps[o + oa + t / ET] - eps[o + ob + t % ET];
   __syncthreads();

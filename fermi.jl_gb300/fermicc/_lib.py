@@ -39,7 +39,8 @@ EXPORTS = ("fcc_default_opts", "fcc_create", "fcc_upload_df", "fcc_upload_conv",
            "fcc_mp2_energy", "fcc_upload_ao_df", "fcc_upload_ao3_df", "fcc_scf_create", "fcc_scf_destroy",
            "fcc_scf_last_error", "fcc_scf_upload_b", "fcc_scf_fit", "fcc_scf_build_fock", "fcc_scf_build_fock_occ")
 TEST_EXPORTS = ("fcc_test_contract", "fcc_stat_launches", "fcc_stream", "fcc_prof_enable", "fcc_prof_read",
-                "fcc_test_set_t3_bn", "fcc_test_split3", "fcc_test_inject", "fcc_test_triples_subset", "fcc_test_set_t3_kc")
+                "fcc_test_set_t3_bn", "fcc_test_split3", "fcc_test_pack_oz", "fcc_test_inject",
+                "fcc_test_triples_subset", "fcc_test_set_t3_kc")
 
 
 class FccOpts(ctypes.Structure):
@@ -130,6 +131,9 @@ def load():
     lib.fcc_test_set_t3_bn.restype = ctypes.c_int
     lib.fcc_test_split3.argtypes = [dp, i64, i64, i32, ctypes.c_double, ctypes.POINTER(ctypes.c_uint16)]
     lib.fcc_test_split3.restype = ctypes.c_int
+    lib.fcc_test_pack_oz.argtypes = [dp, i64, i64, i32, i32, ctypes.POINTER(ctypes.c_uint16),
+                                     ctypes.POINTER(ctypes.c_int32)]
+    lib.fcc_test_pack_oz.restype = ctypes.c_int
     lib.fcc_test_set_t3_kc.argtypes = [vp, i32]
     lib.fcc_test_set_t3_kc.restype = ctypes.c_int
     lib.fcc_test_inject.argtypes = [vp, i32]

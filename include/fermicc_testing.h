@@ -33,6 +33,14 @@ int fcc_test_contract(int32_t precision, const char* spec, const double* A, cons
  * lo(K)] per row. */
 int fcc_test_split3(const double* x, int64_t R, int64_t K, int32_t row_fastest, double scale, uint16_t* out);
 
+/* The exact-slice operand packing on device 0: x is R x K (row-major, or
+ * column-major when row_fastest != 0), cut into S (1..8) signed 6-bit digit
+ * slices; out receives R rows of S * Kpad bf16 bit patterns (Kpad = K
+ * rounded up to 64; slice s at columns [s * Kpad, s * Kpad + K), zeros to
+ * (s + 1) * Kpad) and ex the R biased FP64 exponents of the row maxima. */
+int fcc_test_pack_oz(const double* x, int64_t R, int64_t K, int32_t row_fastest, int32_t S, uint16_t* out,
+                     int32_t* ex);
+
 /* Number of kernels this library has launched in the process so far. */
 int64_t fcc_stat_launches(void);
 
