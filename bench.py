@@ -85,6 +85,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true",
                     help="skip the plain FP64 form (the metric's comparator and the error budget)")
+    ap.add_argument("--switch-rms", type=float, default=None,
+                    help="mixed form: rms at which it leaves the split-BF16 phase (default: the library's)")
     ap.add_argument("--part", default="cc", choices=["cc", "rhf-fock"],
                     help="rhf-fock: time the DF-RHF Fock build and the RHF iterations instead (own JSON line)")
     ap.add_argument("--profile-case", default=None,
@@ -377,6 +379,8 @@ def main():
         Options.set("cc_e_conv", E_CONV)
         Options.set("cc_max_rms", MAX_RMS)
         Options.set("cc_max_iter", 100)
+        if args.switch_rms is not None:
+            Options.set("cc_gpu_switch_rms", args.switch_rms)
 
     set_form(args.form)
     from fermicc.mlp import DEFAULT_PARAMS, MLPGuess
@@ -564,6 +568,7 @@ def main():
                "data": "synthetic (seeded water cluster, stand-in basis)",
                "config": {"workload": f"(H2O){args.waters} seed {args.seed} DF-RCCSD(T)", "form": args.form,
                           "mixed_finish": Options.get("cc_gpu_finish") if args.form == "mixed" else None,
+                          "switch_rms": Options.get("cc_gpu_switch_rms") if args.form == "mixed" else None,
                           "o": inp.o, "v": inp.v, "naux": inp.naux, "e_conv": E_CONV, "max_rms": MAX_RMS,
                           "parallelism": "replicas" if world > 1 else "single GPU",
                           "l2": "working set > L2 (T2 189 MB, factors 160 MB)"},

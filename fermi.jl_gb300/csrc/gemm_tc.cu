@@ -69,7 +69,7 @@ __device__ __forceinline__ uint32_t round8(uint64_t a, int& sh) {
 // (typically ~2^-27; pieces below the bf16 range become zero).  Integer arithmetic on the
 // FP64 bit pattern: the remainders are exact and no FP64 instruction (a slow
 // pipe on this part) is issued.
-__device__ __forceinline__ void split3_int(double x, __nv_bfloat16 (&lv)[3]) {
+__device__ __noinline__ void split3_int(double x, __nv_bfloat16 (&lv)[3]) {
   const uint64_t u = (uint64_t)__double_as_longlong(x);
   const int ex = (int)((u >> 52) & 0x7FF);
   uint16_t h = 0, m = 0, l = 0;
@@ -135,7 +135,8 @@ __device__ __forceinline__ uint64_t piece_units(uint32_t pb, int e0) {
 // arithmetic where every piece is a normal float (2^-74 <= |x| < 2^127, so
 // all pieces, multiples of the FP64 ulp of x, are at least 2^-126): the
 // remainders stay exact 64-bit integers in units of that ulp, and each
-// rounding to 8 bits goes through rne8_bits; other x take split3_int.
+// rounding to 8 bits goes through rne8_bits; other x take split3_int (not
+// inlined, so the common path carries none of its instructions).
 __device__ __forceinline__ void split3(double x, __nv_bfloat16 (&lv)[3]) {
   const uint64_t u = (uint64_t)__double_as_longlong(x);
   const int ex = (int)((u >> 52) & 0x7FF);
