@@ -36,6 +36,25 @@ struct TileTri {
   int16_t a, b, c, pad;
 };
 
+// x = hi + lo, two floats (hi = x rounded, lo = the rest rounded): ~2^-48 relative
+__device__ __forceinline__ float2 split_f2(double x) {
+  const float h = __double2float_rn(x);
+  return make_float2(h, __double2float_rn(x - (double)h));
+}
+// a + b and its rounding error e (Knuth's TwoSum, no condition on the magnitudes)
+__device__ __forceinline__ float two_sum(float a, float b, float& e) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return s;
+}
+// (x.hi + x.lo) - (y.hi + y.lo) rounded to one float
+__device__ __forceinline__ float diff_f2(float2 x, float2 y) {
+  float e;
+  const float s = two_sum(x.x, -y.x, e);
+  return __fadd_rn(s, __fadd_rn(e, __fsub_rn(x.y, y.y)));
+}
+
 // Energy of the triplets (i, j, k0 + blockIdx.y) on the sub-cube
 // tiles[blockIdx.x] (tile blocks A >= B >= C).  part[k * ntiles + tile]
 // accumulates over the calls in a fixed order.
@@ -48,8 +67,8 @@ __global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
   __shared__ float Mik[3][3][ET][ET + 1];
   __shared__ float Mij[3][3][ET][ET + 1];
   __shared__ float T1[3][3][ET];            // t1 of i, j, k on block r
-  __shared__ double epsv[3][ET];
-  __shared__ double Dab[ET][ET];            // e_i + e_j + e_k - e_a - e_b
+  __shared__ float2 ecf[ET];                // e_c of block C as an unevaluated float sum (hi, lo)
+  __shared__ float2 Dabf[ET][ET];           // e_i + e_j + e_k - e_a - e_b likewise
   __shared__ double red[ETH / 32];
   const int kq = blockIdx.y, k = k0 + kq;
   if (i == j && j == k) return;
@@ -125,7 +144,7 @@ __global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
     T1[0][r][x] = X < v ? t1f[(int64_t)i * v + X] : 0.0f;
     T1[1][r][x] = X < v ? t1f[(int64_t)j * v + X] : 0.0f;
     T1[2][r][x] = X < v ? t1f[(int64_t)k * v + X] : 0.0f;
-    epsv[r][x] = X < v ? eps[o + X] : 0.0;
+    if (r == 2) ecf[x] = split_f2(X < v ? eps[o + X] : 0.0);
   }
 #pragma unroll
   for (int q = 0; q < NM; ++q) {
@@ -165,7 +184,8 @@ __global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
     Wt[p][slo + 2][shi][smid] += gv[q].z;
     Wt[p][slo + 3][shi][smid] += gv[q].w;
   }
-  if (t < ET * ET) Dab[t / ET][t % ET] = eps[i] + eps[j] + eps[k] - eps[o + oa + t / ET] - eps[o + ob + t % ET];
+  if (t < ET * ET)
+    Dabf[t / ET][t % ET] = split_f2(eps[i] + eps[j] + eps[k] - eps[o + oa + t / ET] - eps[o + ob + t % ET]);
   __syncthreads();
 
   // V(x,y,z) for x in block rx at lx etc.: W + t1_ix (jy|kz) + (ix|kz) t1_jy + (ix|jy) t1_kz
@@ -187,15 +207,24 @@ __global__ void __launch_bounds__(ETH) triples_energy_tiled_kernel(
     const float Y = Vabc + Vbca + Vcab;
     const float Z = Vacb + Vbac + Vcba;
     const float Ef = (Y - 2.0f * Z) * (Wabc + Wbca + Wcab) + (Z - 2.0f * Y) * (Wacb + Wbac + Wcba) + 3.0f * X;
-    // denominator in FP64; the quotient of the FP32 Ef in FP32 (the FP64 pipe
-    // is 1/64 rate: an FP64 division per (a,b,c) bounded this kernel)
-    const double D = Dab[la][lb] - epsv[2][lc];
+    // denominator from the FP64 orbital energies, carried as float pairs
+    // (~2^-48 relative) and rounded once to FP32; the quotient of the FP32 Ef
+    // in FP32 (the FP64 pipe is 1/64 rate on this part: FP64 denominators
+    // and reductions kept it 35% busy)
+    const float D = diff_f2(Dabf[la][lb], ecf[lc]);
     const float wgt = 1.0f + (float)(a == b) + (float)(b == c);
-    accf += __fdiv_rn(Ef, (float)D * wgt);
+    accf += __fdiv_rn(Ef, D * wgt);
   }
-  double acc = (double)accf;
-  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-  if ((t & 31) == 0) red[t >> 5] = acc;
+  // warp sum in double-float (TwoSum), then FP64 over warps and blocks
+  float sh = accf, sl = 0.0f;
+  for (int off = 16; off > 0; off >>= 1) {
+    const float oh = __shfl_down_sync(0xffffffffu, sh, off), ol = __shfl_down_sync(0xffffffffu, sl, off);
+    float e;
+    const float h = two_sum(sh, oh, e);
+    sl = __fadd_rn(__fadd_rn(sl, ol), e);
+    sh = two_sum(h, sl, sl);
+  }
+  if ((t & 31) == 0) red[t >> 5] = (double)sh + (double)sl;
   __syncthreads();
   if (t == 0) {
     double s = 0.0;
