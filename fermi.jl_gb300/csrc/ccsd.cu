@@ -952,13 +952,15 @@ int ccsd_run(fcc_ctx* c, const fcc_opts* opt, fcc_iter_stats* log, int32_t log_c
         // when the criteria hold ten times over on this iteration and hold on
         // the previous one, so that the FP64 step that follows (whose energy
         // change is the next step of the same convergence) meets them at
-        // once.  Exact-slice finish (about the cost of one more exact-slice
-        // iteration): switch as soon as the criteria hold; a finish step that
-        // misses them is followed by another.
+        // once.  Exact-slice finish (~1.5 exact-slice iterations): switch
+        // once the step is below max_rms with the energy change within ten
+        // times e_conv, i.e. when the next step is expected to meet the
+        // criteria (an exact-slice step that met them would be one wasted
+        // iteration); a finish step that misses them is followed by another.
         const bool ready = finish == K_F64
                                ? (rms < 0.1 * op.max_rms && std::fabs(dE) < 0.1 * op.e_conv &&
                                   std::fabs(prev_dE) < op.e_conv)
-                               : (rms < op.max_rms && std::fabs(dE) < op.e_conv);
+                               : (rms < op.max_rms && std::fabs(dE) < 10.0 * op.e_conv);
         if (ready || stalled >= 5) kind = finish;
       }
     }
