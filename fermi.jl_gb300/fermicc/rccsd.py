@@ -148,10 +148,12 @@ class Context:
         return rc, res, lines
 
     def amplitudes(self):
-        T1 = np.zeros((self.o, self.v), order="F")
-        T2 = np.zeros((self.o, self.o, self.v, self.v), order="F")
+        """T1[i, a] and T2[i, j, a, b] as column-major arrays (Fermi's layout;
+        the ABI writes that layout, so no host-side copy follows)."""
+        T1 = np.empty((self.o, self.v), order="F")
+        T2 = np.empty((self.o, self.o, self.v, self.v), order="F")
         _check(self.lib, self.h, self.lib.fcc_get_amps(self.h, _ptr(T1), _ptr(T2)), "fcc_get_amps")
-        return np.ascontiguousarray(T1), np.ascontiguousarray(T2)
+        return T1, T2
 
     def save_checkpoint(self, path: str):
         """Write the current amplitudes (header + column-major T1, T2)."""
