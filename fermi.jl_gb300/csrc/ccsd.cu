@@ -611,11 +611,66 @@ void residual(fcc_ctx* c) {
     KeepPackedA keep(tc_engine(), c->Tp.p, c->Tm.p);
     auto startP = [&](int64_t a) { return a * v - a * (a - 1) / 2; };   // first (a, b>=a) row
     auto startM = [&](int64_t a) { return a * v - a * (a + 1) / 2; };   // first (a, b>a) row
+    // On the tensor cores every block's (ac|bd) = sum_Q Bt[Q][a][c] Bt[Q][b][d]
+    // takes its rows (a, c) for a in the block and (b, d) for b >= a0 from one
+    // packing of Bt over all (x, y) (row x * v + y, K = Q): two row ranges of
+    // the same packed array, instead of packing both slices for every block.
+    TcEngine* tc = tc_engine();
+    const bool tcw = tc && tc->enabled;
+    const int64_t R = v * v;
+    int64_t Wk = 0;   // packed row length
+    if (tcw) {
+      PackSpec ps{};
+      ps.R = R; ps.K = Q;
+      ps.rd2 = 1; ps.rd3 = v; ps.rs1 = n; ps.rs2 = 0; ps.rs3 = 1;
+      ps.kd2 = 1; ps.kd3 = Q; ps.ks1 = 0; ps.ks2 = 0; ps.ks3 = n * n;
+      if (tc->exact) {
+        const int S = tc->oz_groups - 1;
+        Wk = S * oz_kpad(Q);
+        ps.Kp = Wk;
+        if ((int64_t)c->bvvA.n < R * Wk) c->bvvA.alloc(R * Wk);
+        if ((int64_t)c->bvvEx.n < R) c->bvvEx.alloc(R);
+        pack_oz(Btvv.p, ps, S, c->bvvA.p, c->bvvEx.p, s);
+      } else {
+        Wk = packed_kp(Q, tc->scheme.P);
+        ps.Kp = Wk;
+        ps.P = tc->scheme.P;
+        if ((int64_t)c->bvvA.n < R * Wk) c->bvvA.alloc(R * Wk);
+        if ((int64_t)c->bvvB.n < R * Wk) c->bvvB.alloc(R * Wk);
+        ps.code = tc->scheme.code_a;
+        pack_split(Btvv.p, ps, c->bvvA.p, s);
+        ps.code = tc->scheme.code_b;
+        pack_split(Btvv.p, ps, c->bvvB.p, s);
+      }
+    }
     for (int64_t a0 = 0; a0 < v; a0 += c->ladder_block) {
       const int64_t na = std::min<int64_t>(c->ladder_block, v - a0);
       const int64_t vb = v - a0;
       TView W = rm(c->Wslab.p, {na, v, vb, v});                            // [a][c][b-a0][d]
-      einsum(1.0, "Qac,Qbd->acbd", slice(Btvv, 1, a0, na), slice(Btvv, 1, a0, vb), 0.0, W, s);
+      if (tcw) {
+        EpiMap ep;
+        ep.M = na * v;
+        ep.N = vb * v;
+        ep.ms1 = vb * v;   // W[(a, c)][(b, d)]
+        ep.ns1 = 1;
+        ep.alpha = 1.0; ep.beta = 0.0; ep.C = c->Wslab.p; ep.mode = EPI_F64;
+        const int64_t r0 = a0 * v;
+        if (tc->exact) {
+          const int G = tc->oz_groups;
+          ep.work = 2.0 * (double)ep.M * (double)ep.N * (double)Q * ((double)(G - 1) * (double)G / 2.0);
+          gemm_oz(c->bvvA.p + r0 * Wk, ep.M, c->bvvEx.p + r0, c->bvvA.p + r0 * Wk, ep.N, c->bvvEx.p + r0, Wk / (G - 1),
+                  G, ep, tc->err, s);
+        } else {
+          ep.work = 2.0 * (double)ep.M * (double)ep.N * (double)Q * tc->scheme.P;
+          ep.no_loads = tc->no_loads_once;
+          tc->no_loads_once = 0;
+          gemm_bf16x3(c->bvvA.p, R, r0, c->bvvB.p, R, r0, Wk, ep, tc->err, s);
+        }
+        tc->tc_calls++;
+        tc->tc_flops += ep.work;
+      } else {
+        einsum(1.0, "Qac,Qbd->acbd", slice(Btvv, 1, a0, na), slice(Btvv, 1, a0, vb), 0.0, W, s);
+      }
       const int64_t rP0 = startP(a0), nrP = startP(a0 + na) - rP0;
       const int64_t rM0 = startM(a0), nrM = startM(a0 + na) - rM0;
       build_wpm_kernel<<<grid_for(nrP * nP + nrM * nM), 256, 0, s>>>(c->Wslab.p, (int)v, (int)a0, vb, c->pairP_v.p,

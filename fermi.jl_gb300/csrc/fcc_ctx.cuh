@@ -34,6 +34,11 @@ struct fcc_ctx {
   // symmetric / antisymmetric pp-ladder: pair tables (int2), channels
   fcc::DBuf<int2> pairP_v, pairM_v, pairP_o, pairM_o;   // (x<=y) and (x<y) pairs, row-major
   fcc::DBuf<double> Tp, Tm, Wp, Wm, LXp, LXm;
+  // the dressed factors Bt[Q][x][y] (x, y virtual) packed once per residual
+  // for every block's (ac|bd) product (rows (x, y), K = Q): digit slices and
+  // row exponents, or the split pieces in the A and in the B order
+  fcc::DBuf<__nv_bfloat16> bvvA, bvvB;
+  fcc::DBuf<int> bvvEx;
   // reductions
   fcc::DBuf<double> red;      // device scratch for scalar reductions
   fcc::DBuf<double> f64ws;    // split-K partial sums of the FP64 contractions
