@@ -88,7 +88,7 @@ typedef struct {
   int32_t ite;
   int32_t diis;      /* 1 if this iteration extrapolated                */
   int32_t precision; /* residual of this iteration: 0 FP64, 1 split-BF16, */
-                     /* 2 exact-slice BF16 (Ozaki scheme, 6-8 groups),   */
+                     /* 2 exact-slice BF16 (Ozaki scheme, 6-7 groups),   */
                      /* 3 exact-slice at 9 groups (FP64-accurate)        */
   int32_t pad;
   double energy;     /* correlation energy after the iteration          */
