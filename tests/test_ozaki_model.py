@@ -58,3 +58,26 @@ def test_chunk_sums_stay_exact_in_fp32():
     for p in d[0] * d[1]:
         s = np.float32(s + p)
     assert int(s) == int(np.sum(d[0].astype(np.int64) * d[1].astype(np.int64)))
+
+
+def test_biased_plain_digits_are_the_sequential_cut():
+    # the device cuts Z into balanced digits as the plain base-64 digits of
+    # Z + 32 (64^(S-2) + ... + 1), less 32 (top digit: the rest), with every
+    # shift a constant; the same digits as the sequential cut with carries
+    rng = np.random.default_rng(3)
+    for S in range(1, 9):
+        C = 32 * ((64 ** (S - 1) - 1) // 63)
+        for Z in list(rng.integers(0, 64 ** S + 1, 3000, dtype=np.int64)) + [0, 31, 32, 63, 64, 64 ** S]:
+            Z = int(Z)
+            seq, t = [0] * S, Z
+            for s in range(S - 1, 0, -1):
+                r = t & 63
+                t >>= 6
+                if r >= 32:
+                    r -= 64
+                    t += 1
+                seq[s] = r
+            seq[0] = t
+            Zc = Z + C
+            plain = [Zc >> (6 * (S - 1))] + [((Zc >> (6 * (S - 1 - s))) & 63) - 32 for s in range(1, S)]
+            assert plain == seq, (S, Z)

@@ -45,3 +45,74 @@ def test_exact_small_values_need_one_piece():
         assert sp.bf16_value(h) == v and m == 0 and l == 0
     h, m, l = sp.split3_bits(257.0)          # 9 significant bits: two pieces
     assert sp.bf16_value(h) + sp.bf16_value(m) == 257.0 and l == 0
+
+
+# --- the device's single-precision path (csrc/gemm_tc.cu split3), restated
+# with exact integer emulation of each float operation: the 24-bit cut with
+# rounding to odd, then the float-to-bf16 rounding (nearest, ties to even)
+
+def _bf16_rne_of_float(b32):
+    """bf16 bits of the float with bits b32 (finite), nearest-even."""
+    return ((b32 + 0x7FFF + ((b32 >> 16) & 1)) >> 16) & 0xFFFF
+
+
+def _float_bits(m, e):
+    """bits of the normal float m * 2^e with 2^23 <= m < 2^24."""
+    return ((e + 23 + 127) << 23) | (m & 0x7FFFFF)
+
+
+def _rne8_units(a, e0):
+    """bf16 bits of round8(a * 2^e0) through the round-to-odd float (a > 0)."""
+    n = a.bit_length()
+    if n <= 24:
+        m, sh = a << (24 - n), -(24 - n)
+    else:
+        sh = n - 24
+        m = a >> sh
+        if (m << sh) != a:      # bits lost below the cut: set the last one
+            m |= 1
+    return _bf16_rne_of_float(_float_bits(m, sh + e0))
+
+
+def _units(pb, e0):
+    m8, sh = 0x80 | (pb & 0x7F), ((pb >> 7) & 0xFF) - 134 - e0
+    return m8 << sh if sh >= 0 else m8 >> -sh
+
+
+def _split3_device_model(x):
+    import struct
+    u = struct.unpack("<Q", struct.pack("<d", x))[0]
+    ex = (u >> 52) & 0x7FF
+    if ex < 949 or ex > 1149:                       # the all-integer path
+        return sp.split3_bits(x)
+    sg, e0 = u >> 63, ex - 1075
+    M = (u & ((1 << 52) - 1)) | (1 << 52)
+    hb = _rne8_units(M, e0)
+    r1 = M - _units(hb, e0)
+    m = l = 0
+    if r1:
+        sg1 = sg ^ (r1 < 0)
+        mb = _rne8_units(abs(r1), e0)
+        m = (sg1 << 15) | mb
+        r2 = abs(r1) - _units(mb, e0)
+        if r2:
+            l = ((sg1 ^ (r2 < 0)) << 15) | _rne8_units(abs(r2), e0)
+    return ((sg << 15) | hb, m, l)
+
+
+def test_round_to_odd_path_is_the_integer_model():
+    # cutting the remainder at 24 bits with the last bit set when bits were
+    # lost, then rounding that float to bf16, equals rounding the remainder
+    # itself (Boldo & Melquiond): the device's fast path gives the pieces of
+    # split3_bits bit for bit, ties included
+    rng = np.random.default_rng(11)
+    xs = list(rng.standard_normal(4000) * 10.0 ** rng.uniform(-30, 30, 4000))
+    xs += [1.0 + 2.0 ** -8, 1.0 + 3 * 2.0 ** -8, 257.0, 1.0 + 2.0 ** -9 + 2.0 ** -17, 1.0 + 2.0 ** -16 + 2.0 ** -25,
+           2.0 ** -74, 1.7 * 2.0 ** -73, 1.9 * 2.0 ** 126, -1.5 * 2.0 ** 127, 1.0 / 3.0, -255.0]
+    for _ in range(2000):                                               # exact ties below hi and mid
+        base = int(rng.integers(128, 256))
+        k = int(rng.integers(0, 27))
+        M = (base << 45) + (int(rng.integers(128, 256)) << (36 - k)) + (1 << (35 - k))
+        xs.append(float(np.ldexp(float(M), int(rng.integers(-100, 60)) - 52)))
+    for x in xs:
+        assert _split3_device_model(float(x)) == sp.split3_bits(float(x)), x
